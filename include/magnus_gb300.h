@@ -1,0 +1,133 @@
+/* magnus_gb300.h — C ABI of the GB300 Magnus-expansion engine.
+ *
+ * The engine computes the Magnus terms Omega_1..Omega_n of a sampled matrix
+ * function A(t_i), i = 0..S-1 on [t0, tf] (dt = (tf - t0) / (S - 1)), and
+ * their vector-Jacobian products, on one NVIDIA GB300 GPU.  Every entry point
+ * takes plain pointers and sizes; none throws; each returns an mgb_status and
+ * leaves a message retrievable with mgb_last_error() (per calling thread).
+ *
+ * Buffer conventions (C-contiguous, row-major, element type = problem dtype):
+ *   matrix kind      A   (S, d, d)          out  (d, d) | (n, d, d) for op=many
+ *                    dA  (S, d, d)          cot  shape of out
+ *   spacecurve kind  A   (S, 3)             out  (3,)   | (n, 3)
+ *                    dA  (S, 3)             cot  shape of out
+ *   carry (record_vjp) (Q, n-1, S, d, d) with Q = (n+3)/2 (spacecurve: d=2),
+ *     element ((q*(n-1) + k-2)*S + i) holds the prefix P_k[i] of GL node q,
+ *     exactly the reference's VJP::Data layout.
+ *
+ * Device entry points (mgb_forward, mgb_vjp, *_batched) take DEVICE pointers
+ * and a cudaStream_t (as void*, NULL = legacy default stream); they are
+ * stream-ordered and return before the GPU work completes.  Host entry
+ * points (*_host) take host pointers and are synchronous.
+ *
+ * Reference interfaces replaced (paths in s-cavalier/magnus-dp):
+ *   mgb_forward      <- Magnus::detail::run_raw_impl            src/composer/backends.hpp:182-220
+ *                       and run_spacecurve_raw_impl             src/composer/backends.hpp:253-301
+ *                       (KernelPlan::run of make_plan,          src/composer/backends.cpp:65-93)
+ *   mgb_vjp          <- Magnus::detail::run_vjp_raw_impl        src/composer/backends.hpp:222-251
+ *                       and run_spacecurve_vjp_raw_impl         src/composer/backends.hpp:303-357
+ *                       (KernelPlan::run of make_vjp_plan,      src/composer/backends.cpp:95-102)
+ *   mgb_*_host       <- _core.compute / compute_sc / compute_vjp / compute_sc_vjp
+ *                                                               src/api/pybind.cpp:357-433
+ *   mgb_set_gl_table <- Magnus::detail::replace_gl_table        src/api/pybind.cpp:102-116
+ *   mgb_max_order    <- Magnus::detail::max_order               src/api/pybind.cpp:57-59
+ *   error strings    <- std::invalid_argument messages of       src/composer/backends.hpp:108-180,
+ *                                                               src/composer/backends.cpp:37-53,
+ *                                                               src/composer/dispatch.hpp:119-183
+ */
+#ifndef MAGNUS_GB300_H
+#define MAGNUS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mgb_status {
+    MGB_OK = 0,
+    MGB_ERR_INVALID_ARGUMENT = 1, /* maps to ValueError / std::invalid_argument */
+    MGB_ERR_TYPE = 2,             /* maps to TypeError */
+    MGB_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    MGB_ERR_OUT_OF_MEMORY = 4,
+    MGB_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait gave up */
+} mgb_status;
+
+enum { MGB_KIND_MATRIX = 0, MGB_KIND_SPACECURVE = 1 };
+enum { MGB_DTYPE_F32 = 0, MGB_DTYPE_F64 = 1 };
+/* PLAIN: every product and sum in FP64 (parity form, <=1e-12 vs the reference).
+ * MIXED: per-sample products and in-chunk prefixes in FP32, chunk carries,
+ *        scans and the final Omega assembly in FP64. */
+enum { MGB_PRECISION_PLAIN = 0, MGB_PRECISION_MIXED = 1 };
+enum { MGB_OP_ONE = 0, MGB_OP_MANY = 1, MGB_OP_SUM = 2 };
+enum { MGB_INTEGRATOR_BOOLE = 0, MGB_INTEGRATOR_SIMPSON = 1, MGB_INTEGRATOR_TRAPEZOID = 2, MGB_INTEGRATOR_RIEMANN = 3 };
+
+typedef struct mgb_problem {
+    int32_t kind;          /* MGB_KIND_* */
+    int32_t dtype;         /* MGB_DTYPE_* : element type of every buffer */
+    int32_t precision;     /* MGB_PRECISION_* */
+    int32_t op;            /* MGB_OP_* */
+    int32_t integrator;    /* MGB_INTEGRATOR_* */
+    uint32_t checkpoint_K; /* samples per checkpoint chunk; 0 = engine default; else a multiple of 4 */
+    uint64_t n;            /* Magnus order, >= 1 */
+    uint64_t samples;      /* S, >= 2 */
+    uint64_t dim;          /* d (ignored for spacecurve) */
+    double t0;
+    double tf;
+} mgb_problem;
+
+/* Forward: out <- op(Omega_1..Omega_n).  carry (nullable): reference-format
+ * prefix record.  ckpt (nullable): engine checkpoints (mgb_checkpoint_bytes)
+ * that a later mgb_vjp can reuse instead of recomputing the forward scan. */
+mgb_status mgb_forward(const mgb_problem* p, const void* A, void* out, void* carry, void* ckpt, void* stream);
+
+/* VJP: dA <- d<cot, op(Omega)>/dA (bilinear pairing, as the reference).
+ * ckpt: buffer written by mgb_forward for the same problem and A, or NULL to
+ * recompute the forward checkpoints. */
+mgb_status mgb_vjp(const mgb_problem* p, const void* A, const void* cot, const void* ckpt, void* dA, void* stream);
+
+/* Bytes of the checkpoint buffer for problem p (0 on invalid p). */
+size_t mgb_checkpoint_bytes(const mgb_problem* p);
+
+/* Batched forms: `count` independent instances in one set of launches.
+ * Instances may differ in n, samples, dim, op, t0, tf and checkpoint_K; they
+ * must share kind, dtype, precision and integrator.  ckpt may be NULL (the
+ * array) or hold NULL entries. */
+mgb_status mgb_forward_batched(const mgb_problem* probs, size_t count, const void* const* A, void* const* out,
+                               void* const* ckpt, void* stream);
+mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* const* A, const void* const* cot,
+                           const void* const* ckpt, void* const* dA, void* stream);
+
+/* Host-pointer forms (synchronous; device staging inside). carry nullable. */
+mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void* carry);
+mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, void* dA);
+
+/* Gauss-Legendre table: weights/nodes on [0, 1] for orders 1..max_order,
+ * order q at offset q(q-1)/2 (flattened like the reference).  Copied. */
+mgb_status mgb_set_gl_table(size_t max_order, const double* weights, const double* nodes);
+size_t mgb_max_order(void);
+
+/* Kernel timing.  While enabled, every engine kernel launch is bracketed by
+ * CUDA events on its stream; mgb_profile_read waits for the recorded events,
+ * fills up to `capacity` entries (one per kernel name: launches and total
+ * milliseconds) and returns the number of names.  For benchmarking only: the
+ * events add a few microseconds per launch.  No reference counterpart (the
+ * reference has no tracing). */
+typedef struct mgb_kernel_time {
+    char name[40];
+    uint64_t launches;
+    double total_ms;
+} mgb_kernel_time;
+mgb_status mgb_profile_enable(int enable);
+size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset);
+
+/* Message of the last non-OK status on the calling thread ("" if none). */
+const char* mgb_last_error(void);
+int mgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGNUS_GB300_H */

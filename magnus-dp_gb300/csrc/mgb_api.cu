@@ -1,0 +1,596 @@
+// C ABI of the engine (declared in include/magnus_gb300.h): validation with
+// the reference's error contract, call planning, a stream-ordered workspace,
+// and the kernel launch sequences for forward and VJP.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "magnus_gb300.h"
+#include "mgb_kernels.h"
+#include "mgb_tuned.h"
+#include "gl_table.inc"
+
+namespace {
+
+using namespace mgb;
+
+thread_local std::string g_last_error;
+
+mgb_status fail(mgb_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+// ---------------------------------------------------------------- GL table
+struct GLData {
+    size_t max_order;
+    std::vector<double> w, x;
+};
+
+std::mutex g_gl_mutex;
+std::shared_ptr<const GLData> g_gl;
+
+std::shared_ptr<const GLData> gl_snapshot() {
+    std::lock_guard<std::mutex> lock(g_gl_mutex);
+    if (!g_gl) {
+        auto t = std::make_shared<GLData>();
+        t->max_order = MGB_GL_DEFAULT_MAX_ORDER;
+        size_t cnt = sizeof(mgb_gl_default_nodes) / sizeof(double);
+        t->x.assign(mgb_gl_default_nodes, mgb_gl_default_nodes + cnt);
+        t->w.assign(mgb_gl_default_weights, mgb_gl_default_weights + cnt);
+        g_gl = t;
+    }
+    return g_gl;
+}
+
+// ---------------------------------------------------------------- profiler
+struct ProfEvent {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+struct ProfTotal {
+    uint64_t launches = 0;
+    double ms = 0.0;
+};
+std::mutex g_prof_mutex;
+bool g_prof_enabled = false;
+std::vector<ProfEvent> g_prof_pending;
+std::vector<std::pair<std::string, ProfTotal>> g_prof_totals;
+
+bool prof_on() {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    return g_prof_enabled;
+}
+
+template <class F>
+cudaError_t timed(const char* name, cudaStream_t st, F&& fn) {
+    if (!prof_on()) return fn();
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, st);
+    cudaError_t e = fn();
+    cudaEventRecord(b, st);
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    g_prof_pending.push_back(ProfEvent{name, a, b});
+    return e;
+}
+
+// ---------------------------------------------------------------- devices
+struct DevInfo {
+    int sms = 0;
+};
+
+DevInfo device_info() {
+    static std::mutex mu;
+    static std::vector<DevInfo> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1);
+    if (cache[dev].sms == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev].sms = sms > 0 ? sms : 1;
+    }
+    return cache[dev];
+}
+
+// ---------------------------------------------------------------- validation
+struct Derived {
+    int m, Q, C, K, div;
+    int64_t nm;
+};
+
+int rule_divisibility(int integrator) {
+    switch (integrator) {
+        case MGB_INTEGRATOR_BOOLE: return 4;
+        case MGB_INTEGRATOR_SIMPSON: return 2;
+        case MGB_INTEGRATOR_TRAPEZOID: return 2;
+        default: return 1;
+    }
+}
+
+int default_K(const mgb_problem& p) {
+    if (p.kind == MGB_KIND_SPACECURVE || p.dim <= 32) return 256;
+    if (p.dim <= 64) return 128;
+    return 64;
+}
+
+// Mirrors Magnus::detail::matrix_input_shape / spacecurve_input_shape
+// (src/composer/backends.hpp:108-137) and dispatch_plan's checks
+// (src/composer/backends.cpp:37-53).
+mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
+    if (!p) return fail(MGB_ERR_INVALID_ARGUMENT, "problem must not be null");
+    if (p->n == 0) return fail(MGB_ERR_INVALID_ARGUMENT, "n must be at least 1");
+    if (p->kind != MGB_KIND_MATRIX && p->kind != MGB_KIND_SPACECURVE)
+        return fail(MGB_ERR_INVALID_ARGUMENT, "invalid dispatch option (based on params)");
+    if (p->dtype != MGB_DTYPE_F32 && p->dtype != MGB_DTYPE_F64)
+        return fail(MGB_ERR_TYPE, "magnus only supports dtypes float32, float64, complex64, and complex128");
+    if (p->precision != MGB_PRECISION_PLAIN && p->precision != MGB_PRECISION_MIXED)
+        return fail(MGB_ERR_INVALID_ARGUMENT, "invalid dispatch option (based on params)");
+    if (p->op < MGB_OP_ONE || p->op > MGB_OP_SUM)
+        return fail(MGB_ERR_INVALID_ARGUMENT,
+                    "could not deduce kernel op from str in Magnus::Dispatch::op_from_str(std::string_view)");
+    if (p->integrator < MGB_INTEGRATOR_BOOLE || p->integrator > MGB_INTEGRATOR_RIEMANN)
+        return fail(MGB_ERR_INVALID_ARGUMENT, "Could not resolve dispatch name option");
+    if (p->samples < 2) return fail(MGB_ERR_INVALID_ARGUMENT, "data must contain at least two samples");
+    if (p->kind == MGB_KIND_MATRIX && p->dim == 0) return fail(MGB_ERR_INVALID_ARGUMENT, "data must contain square matrices");
+    const uint64_t d = (p->kind == MGB_KIND_SPACECURVE) ? 2 : p->dim;
+    if (d > 4096) return fail(MGB_ERR_INVALID_ARGUMENT, "matrix dimension is too large");
+    if (p->n > 1 && (p->n + 3) / 2 > gl_max)
+        return fail(MGB_ERR_INVALID_ARGUMENT, "requested magnus order exceeds GL table. Consider providing a larger table.");
+    if (p->n > 4096) return fail(MGB_ERR_INVALID_ARGUMENT, "requested magnus order exceeds GL table. Consider providing a larger table.");
+    const int div = rule_divisibility(p->integrator);
+    if ((p->samples - 1) % (uint64_t)div != 0)
+        return fail(MGB_ERR_INVALID_ARGUMENT,
+                    "sample interval count violates integrator divisibility (a power of 2 is recommneded; i.e., total "
+                    "samples is 2^k + 1 for some k > 4)");
+    if (p->samples > (uint64_t)std::numeric_limits<int64_t>::max() / (d * d + 1))
+        return fail(MGB_ERR_INVALID_ARGUMENT, "input shape is too large");
+    int K = p->checkpoint_K ? (int)p->checkpoint_K : default_K(*p);
+    if (K < 4 || K % 4 != 0 || K > (1 << 20))
+        return fail(MGB_ERR_INVALID_ARGUMENT, "checkpoint_K must be a positive multiple of 4");
+    dv->m = (int)(d * d);
+    dv->Q = p->n > 1 ? (int)((p->n + 3) / 2) : 1;
+    dv->K = K;
+    dv->C = (int)((p->samples - 1 + K - 1) / K);
+    dv->div = div;
+    dv->nm = (int64_t)p->n * dv->m;
+    return MGB_OK;
+}
+
+size_t ckpt_doubles(const mgb_problem& p, const Derived& dv) { return (size_t)(2 * dv.C + 1) * dv.nm; }
+size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + (size_t)dv.Q * dv.nm + 5 * (size_t)dv.nm; }
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---------------------------------------------------------------- workspace
+struct Workspace {
+    void* base = nullptr;
+    cudaStream_t st = nullptr;
+    ~Workspace() {
+        if (base) cudaFreeAsync(base, st);
+    }
+};
+
+#define MGB_CUDA_TRY(expr)                                                                         \
+    do {                                                                                           \
+        cudaError_t e_ = (expr);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            if (e_ == cudaErrorMemoryAllocation) {                                                 \
+                cudaGetLastError();                                                                \
+                return fail(MGB_ERR_OUT_OF_MEMORY, std::string("CUDA out of memory: ") + #expr);   \
+            }                                                                                      \
+            return fail(MGB_ERR_CUDA, std::string(cudaGetErrorString(e_)) + " in " + #expr);       \
+        }                                                                                          \
+    } while (0)
+
+struct Call {
+    bool vjp;
+    size_t count;
+    const mgb_problem* probs;
+    const void* const* A;
+    void* const* out;      // forward
+    void* const* carry;    // forward, nullable array
+    void* const* ckpt_out; // forward, nullable array
+    const void* const* cot;      // vjp
+    const void* const* ckpt_in;  // vjp, nullable array
+    void* const* dA;             // vjp
+    cudaStream_t stream;
+};
+
+mgb_status run(const Call& call) {
+    if (call.count == 0) return MGB_OK;
+    if (!call.probs || !call.A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+    auto gl = gl_snapshot();
+    std::vector<Derived> dv(call.count);
+    for (size_t i = 0; i < call.count; ++i) {
+        mgb_status st = validate(&call.probs[i], gl->max_order, &dv[i]);
+        if (st != MGB_OK) return st;
+        const mgb_problem& p0 = call.probs[0];
+        const mgb_problem& p = call.probs[i];
+        if (p.kind != p0.kind || p.dtype != p0.dtype || p.precision != p0.precision || p.integrator != p0.integrator)
+            return fail(MGB_ERR_INVALID_ARGUMENT, "batched instances must share kind, dtype, precision and integrator");
+        if (!call.A[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+        if (!call.vjp && (!call.out || !call.out[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+        if (call.vjp && (!call.cot || !call.cot[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent buffer must not be null");
+        if (call.vjp && (!call.dA || !call.dA[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    }
+    const mgb_problem& p0 = call.probs[0];
+    const int kind = p0.kind;
+    const bool plain = p0.precision == MGB_PRECISION_PLAIN;
+    const int f64io = p0.dtype == MGB_DTYPE_F64;
+    const size_t tsz = plain ? sizeof(double) : sizeof(float);
+
+    // ---- sizes
+    const size_t n_inst = call.count;
+    size_t nwork = 0, gl_doubles = 0, ck_doubles = 0, wsd = 0;
+    int64_t slot_elems = 0;
+    bool any_carry = false;
+    for (size_t i = 0; i < n_inst; ++i) {
+        const mgb_problem& p = call.probs[i];
+        nwork += (size_t)dv[i].C;
+        gl_doubles += 2 * (size_t)dv[i].Q;
+        const bool user_ck = call.vjp ? (call.ckpt_in && call.ckpt_in[i]) : (call.ckpt_out && call.ckpt_out[i]);
+        if (!user_ck) ck_doubles += ckpt_doubles(p, dv[i]);
+        wsd += ws_doubles(dv[i]);
+        const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
+        slot_elems = std::max<int64_t>(slot_elems, (int64_t)(p.n + 4) * L * dv[i].m);
+        if (!call.vjp && call.carry && call.carry[i]) any_carry = true;
+    }
+    if (nwork > (size_t)std::numeric_limits<int32_t>::max()) return fail(MGB_ERR_INVALID_ARGUMENT, "input shape is too large");
+
+    const DevInfo di = device_info();
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 4, (size_t)16 << 30));
+    const size_t slot_bytes = (size_t)slot_elems * tsz;
+    int64_t grid = std::min<int64_t>((int64_t)nwork, (int64_t)di.sms * 8);
+    grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)(budget / std::max<size_t>(slot_bytes, 1))));
+
+    size_t off = 0;
+    const size_t off_inst = off; off = align_up(off + n_inst * sizeof(InstDev), 256);
+    const size_t off_work = off; off = align_up(off + nwork * sizeof(ChunkRef), 256);
+    const size_t off_gl = off; off = align_up(off + gl_doubles * sizeof(double), 256);
+    const size_t off_ck = off; off = align_up(off + ck_doubles * sizeof(double), 256);
+    const size_t off_ws = off; off = align_up(off + wsd * sizeof(double), 256);
+    const size_t off_scr = off; off = align_up(off + (size_t)grid * slot_bytes, 256);
+    const size_t total = off;
+
+    Workspace ws;
+    ws.st = call.stream;
+    MGB_CUDA_TRY(cudaMallocAsync(&ws.base, total, call.stream));
+    char* base = static_cast<char*>(ws.base);
+
+    // ---- host descriptors
+    std::vector<InstDev> hi(n_inst);
+    std::vector<ChunkRef> hw(nwork);
+    std::vector<double> hgl(gl_doubles);
+    size_t wpos = 0, glpos = 0, ckpos = 0, wspos = 0;
+    for (size_t i = 0; i < n_inst; ++i) {
+        const mgb_problem& p = call.probs[i];
+        const Derived& v = dv[i];
+        InstDev& I = hi[i];
+        std::memset(&I, 0, sizeof(I));
+        I.A = call.A[i];
+        if (!call.vjp) {
+            I.out = call.out[i];
+            I.carry = (call.carry && call.carry[i]) ? call.carry[i] : nullptr;
+        } else {
+            I.cot = call.cot[i];
+            I.dA = call.dA[i];
+        }
+        double* ck;
+        const bool user_ck = call.vjp ? (call.ckpt_in && call.ckpt_in[i]) : (call.ckpt_out && call.ckpt_out[i]);
+        if (user_ck) {
+            ck = static_cast<double*>(call.vjp ? const_cast<void*>(call.ckpt_in[i]) : call.ckpt_out[i]);
+        } else {
+            ck = reinterpret_cast<double*>(base + off_ck) + ckpos;
+            ckpos += ckpt_doubles(p, v);
+        }
+        I.pi = ck;
+        I.lam = ck + (size_t)(v.C + 1) * v.nm;
+        double* w = reinterpret_cast<double*>(base + off_ws) + wspos;
+        wspos += ws_doubles(v);
+        I.rho = w; w += (size_t)v.C * v.nm;
+        I.dq = w; w += (size_t)v.Q * v.nm;
+        I.ee = w; w += v.nm;
+        I.tau = w; w += v.nm;
+        I.ob = w; w += v.nm;
+        I.eb = w; w += v.nm;
+        I.db = w; w += v.nm;
+        double* g = reinterpret_cast<double*>(base + off_gl) + glpos;
+        const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
+        for (int q = 0; q < v.Q; ++q) {
+            hgl[glpos + q] = gl->w[go + q];
+            hgl[glpos + v.Q + q] = gl->x[go + q];
+        }
+        I.glw = g;
+        I.glx = g + v.Q;
+        glpos += 2 * (size_t)v.Q;
+        I.dt = (p.tf - p.t0) / (double)(p.samples - 1);
+        I.S = (int64_t)p.samples;
+        I.d = (p.kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p.dim;
+        I.m = v.m;
+        I.n = (int32_t)p.n;
+        I.C = v.C;
+        I.Q = v.Q;
+        I.K = v.K;
+        I.op = p.op;
+        for (int c = 0; c < v.C; ++c) hw[wpos++] = ChunkRef{(int32_t)i, c};
+    }
+    InstDev* d_inst = reinterpret_cast<InstDev*>(base + off_inst);
+    ChunkRef* d_work = reinterpret_cast<ChunkRef*>(base + off_work);
+    MGB_CUDA_TRY(cudaMemcpyAsync(d_inst, hi.data(), n_inst * sizeof(InstDev), cudaMemcpyHostToDevice, call.stream));
+    MGB_CUDA_TRY(cudaMemcpyAsync(d_work, hw.data(), nwork * sizeof(ChunkRef), cudaMemcpyHostToDevice, call.stream));
+    MGB_CUDA_TRY(cudaMemcpyAsync(base + off_gl, hgl.data(), gl_doubles * sizeof(double), cudaMemcpyHostToDevice, call.stream));
+    // pageable copies above are staged before return; host vectors may go.
+    MGB_CUDA_TRY(cudaStreamSynchronize(call.stream));
+
+    LaunchArgs la;
+    la.insts = d_inst;
+    la.work = d_work;
+    la.nwork = (int64_t)nwork;
+    la.scratch = base + off_scr;
+    la.slot_elems = slot_elems;
+    la.grid = grid;
+    la.f64io = f64io;
+    la.stream = call.stream;
+    const int rule = p0.integrator;
+    const int cnt = (int)n_inst;
+
+    const bool need_fwd_scan = !call.vjp || !(call.ckpt_in);
+    bool all_ck_in = call.vjp && call.ckpt_in;
+    if (all_ck_in)
+        for (size_t i = 0; i < n_inst; ++i) all_ck_in = all_ck_in && call.ckpt_in[i];
+    if (!call.vjp || !all_ck_in) {
+        (void)need_fwd_scan;
+        MGB_CUDA_TRY(timed("chunk_local", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_LOCAL, la, hi, di.sms); }));
+        MGB_CUDA_TRY(timed("scan", call.stream, [&] { return launch_small(plain, kind, SMALL_SCAN, d_inst, cnt, f64io, 0, call.stream); }));
+    }
+    MGB_CUDA_TRY(timed("fin_fwd", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_FWD, d_inst, cnt, f64io, call.vjp ? 0 : 1, call.stream); }));
+    if (!call.vjp) {
+        if (any_carry) MGB_CUDA_TRY(timed("chunk_carry", call.stream, [&] { return launch_generic_chunk(plain, kind, rule, MODE_CARRY, la); }));
+    } else {
+        MGB_CUDA_TRY(timed("fin_vjp", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_VJP, d_inst, cnt, f64io, 0, call.stream); }));
+        MGB_CUDA_TRY(timed("rscan", call.stream, [&] { return launch_small(plain, kind, SMALL_RSCAN, d_inst, cnt, f64io, 0, call.stream); }));
+        MGB_CUDA_TRY(timed("chunk_vjp", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_VJP, la, hi, di.sms); }));
+    }
+    return MGB_OK;
+}
+
+}  // namespace
+
+namespace mgb {
+// Chooses the fastest chunk kernel available for the call: the tuned
+// family when every instance has a shape it covers, else the generic one.
+cudaError_t launch_chunk_any(bool plain, int kind, int rule, int mode, const LaunchArgs& a,
+                             const std::vector<InstDev>& hi, int sms) {
+    TunedChoice tc = choose_tuned(plain, kind, rule, mode, a.f64io != 0, hi);
+    if (tc.use) return launch_tuned(tc, plain, kind, rule, mode, a, sms);
+    return launch_generic_chunk(plain, kind, rule, mode, a);
+}
+}  // namespace mgb
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+mgb_status mgb_forward(const mgb_problem* p, const void* A, void* out, void* carry, void* ckpt, void* stream) {
+    g_last_error.clear();
+    void* outs[1] = {out};
+    void* carries[1] = {carry};
+    void* cks[1] = {ckpt};
+    Call c{};
+    c.vjp = false;
+    c.count = 1;
+    c.probs = p;
+    c.A = &A;
+    c.out = outs;
+    c.carry = carries;
+    c.ckpt_out = cks;
+    c.stream = static_cast<cudaStream_t>(stream);
+    return run(c);
+}
+
+mgb_status mgb_vjp(const mgb_problem* p, const void* A, const void* cot, const void* ckpt, void* dA, void* stream) {
+    g_last_error.clear();
+    const void* cots[1] = {cot};
+    const void* cks[1] = {ckpt};
+    void* das[1] = {dA};
+    Call c{};
+    c.vjp = true;
+    c.count = 1;
+    c.probs = p;
+    c.A = &A;
+    c.cot = cots;
+    c.ckpt_in = cks;
+    c.dA = das;
+    c.stream = static_cast<cudaStream_t>(stream);
+    return run(c);
+}
+
+size_t mgb_checkpoint_bytes(const mgb_problem* p) {
+    Derived dv;
+    std::string saved = g_last_error;
+    mgb_status st = validate(p, gl_snapshot()->max_order, &dv);
+    g_last_error = saved;
+    if (st != MGB_OK) return 0;
+    return ckpt_doubles(*p, dv) * sizeof(double);
+}
+
+mgb_status mgb_forward_batched(const mgb_problem* probs, size_t count, const void* const* A, void* const* out,
+                               void* const* ckpt, void* stream) {
+    g_last_error.clear();
+    Call c{};
+    c.vjp = false;
+    c.count = count;
+    c.probs = probs;
+    c.A = A;
+    c.out = out;
+    c.carry = nullptr;
+    c.ckpt_out = ckpt;
+    c.stream = static_cast<cudaStream_t>(stream);
+    return run(c);
+}
+
+mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* const* A, const void* const* cot,
+                           const void* const* ckpt, void* const* dA, void* stream) {
+    g_last_error.clear();
+    Call c{};
+    c.vjp = true;
+    c.count = count;
+    c.probs = probs;
+    c.A = A;
+    c.cot = cot;
+    c.ckpt_in = ckpt;
+    c.dA = dA;
+    c.stream = static_cast<cudaStream_t>(stream);
+    return run(c);
+}
+
+static size_t elem_size(const mgb_problem* p) { return p->dtype == MGB_DTYPE_F64 ? 8 : 4; }
+
+static void sizes_of(const mgb_problem* p, size_t* in_elems, size_t* out_elems, size_t* carry_elems) {
+    const size_t m = p->kind == MGB_KIND_SPACECURVE ? 4 : (size_t)(p->dim * p->dim);
+    const size_t mi = p->kind == MGB_KIND_SPACECURVE ? 3 : m;
+    *in_elems = (size_t)p->samples * mi;
+    *out_elems = (p->op == MGB_OP_MANY ? (size_t)p->n : 1) * mi;
+    const size_t Q = p->n > 1 ? (size_t)(p->n + 3) / 2 : 1;
+    *carry_elems = p->n > 1 ? Q * (size_t)(p->n - 1) * (size_t)p->samples * m : 0;
+}
+
+mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void* carry) {
+    g_last_error.clear();
+    Derived dv;
+    mgb_status st = validate(p, gl_snapshot()->max_order, &dv);
+    if (st != MGB_OK) return st;
+    if (!A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+    if (!out) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    size_t ni, no, nc;
+    sizes_of(p, &ni, &no, &nc);
+    const size_t es = elem_size(p);
+    void *dA_ = nullptr, *dO = nullptr, *dC = nullptr;
+    auto cleanup = [&]() {
+        if (dA_) cudaFree(dA_);
+        if (dO) cudaFree(dO);
+        if (dC) cudaFree(dC);
+    };
+    cudaError_t e = cudaMalloc(&dA_, ni * es);
+    if (e == cudaSuccess) e = cudaMalloc(&dO, no * es);
+    if (e == cudaSuccess && carry && nc) e = cudaMalloc(&dC, nc * es);
+    if (e == cudaSuccess) e = cudaMemcpy(dA_, A, ni * es, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cleanup();
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? MGB_ERR_OUT_OF_MEMORY : MGB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    st = mgb_forward(p, dA_, dO, dC, nullptr, nullptr);
+    if (st == MGB_OK) {
+        e = cudaMemcpy(out, dO, no * es, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && dC) e = cudaMemcpy(carry, dC, nc * es, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cleanup();
+    return st;
+}
+
+mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, void* dA) {
+    g_last_error.clear();
+    Derived dv;
+    mgb_status st = validate(p, gl_snapshot()->max_order, &dv);
+    if (st != MGB_OK) return st;
+    if (!A || !cot) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+    if (!dA) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    size_t ni, no, nc;
+    sizes_of(p, &ni, &no, &nc);
+    const size_t es = elem_size(p);
+    void *dIn = nullptr, *dCot = nullptr, *dOut = nullptr;
+    auto cleanup = [&]() {
+        if (dIn) cudaFree(dIn);
+        if (dCot) cudaFree(dCot);
+        if (dOut) cudaFree(dOut);
+    };
+    cudaError_t e = cudaMalloc(&dIn, ni * es);
+    if (e == cudaSuccess) e = cudaMalloc(&dCot, no * es);
+    if (e == cudaSuccess) e = cudaMalloc(&dOut, ni * es);
+    if (e == cudaSuccess) e = cudaMemcpy(dIn, A, ni * es, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dCot, cot, no * es, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cleanup();
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? MGB_ERR_OUT_OF_MEMORY : MGB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    st = mgb_vjp(p, dIn, dCot, nullptr, dOut, nullptr);
+    if (st == MGB_OK) {
+        e = cudaMemcpy(dA, dOut, ni * es, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) st = fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cleanup();
+    return st;
+}
+
+mgb_status mgb_set_gl_table(size_t max_order, const double* weights, const double* nodes) {
+    g_last_error.clear();
+    if (max_order == 0) return fail(MGB_ERR_INVALID_ARGUMENT, "max_order must be at least 1");
+    if (max_order > 4096) return fail(MGB_ERR_INVALID_ARGUMENT, "max_order is too large");
+    if (!weights || !nodes) return fail(MGB_ERR_INVALID_ARGUMENT, "GL data must not be null");
+    const size_t cnt = max_order * (max_order + 1) / 2;
+    auto t = std::make_shared<GLData>();
+    t->max_order = max_order;
+    t->w.assign(weights, weights + cnt);
+    t->x.assign(nodes, nodes + cnt);
+    std::lock_guard<std::mutex> lock(g_gl_mutex);
+    g_gl = t;
+    return MGB_OK;
+}
+
+size_t mgb_max_order(void) { return gl_snapshot()->max_order; }
+
+const char* mgb_last_error(void) { return g_last_error.c_str(); }
+
+mgb_status mgb_profile_enable(int enable) {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    g_prof_enabled = enable != 0;
+    return MGB_OK;
+}
+
+size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset) {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    for (auto& ev : g_prof_pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(ev.stop) == cudaSuccess && cudaEventElapsedTime(&ms, ev.start, ev.stop) == cudaSuccess) {
+            auto it = std::find_if(g_prof_totals.begin(), g_prof_totals.end(),
+                                   [&](const std::pair<std::string, ProfTotal>& t) { return t.first == ev.name; });
+            if (it == g_prof_totals.end()) {
+                g_prof_totals.push_back({ev.name, ProfTotal{}});
+                it = g_prof_totals.end() - 1;
+            }
+            it->second.launches += 1;
+            it->second.ms += ms;
+        }
+        cudaEventDestroy(ev.start);
+        cudaEventDestroy(ev.stop);
+    }
+    g_prof_pending.clear();
+    size_t count = g_prof_totals.size();
+    for (size_t i = 0; i < count && i < capacity && out; ++i) {
+        std::memset(out[i].name, 0, sizeof(out[i].name));
+        std::strncpy(out[i].name, g_prof_totals[i].first.c_str(), sizeof(out[i].name) - 1);
+        out[i].launches = g_prof_totals[i].second.launches;
+        out[i].total_ms = g_prof_totals[i].second.ms;
+    }
+    if (reset) g_prof_totals.clear();
+    return count;
+}
+
+int mgb_version(void) { return 1; }
+
+}  // extern "C"

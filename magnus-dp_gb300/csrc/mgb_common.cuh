@@ -1,0 +1,312 @@
+// Device-side building blocks shared by all engine kernels.
+//
+// Algorithm (one instance; S samples A_i, order n, dt = (tf-t0)/(S-1)):
+//   The reference runs, for each of Q = (n+3)/2 Gauss-Legendre nodes x_q,
+//   Y_1 = A, Y_k[i] = A[i] (P_k[i] + s T_k) with P_k = prefix(Y_{k-1}),
+//   T_k = P_k[S-1], s = x_q - 1 (src/magnus.hpp:60-84).  Because prefix is
+//   linear and commutes with right-multiplication by constants, every Y_k is
+//   Y_k = sum_j W_j D_{k-j+1} with node-independent "levels"
+//       W_1 = A,  P_j = prefix(W_j),  W_{j+1}[i] = A[i] P_j[i],
+//   and small per-node coefficients D_1 = 1, D_m = s sum_{j<m} T_j D_{m-j}.
+//   For all four block rules the rule's weighted sum equals its prefix total,
+//   dt * sum_w(W_j) = P_j[S-1] = T_j, so
+//       Omega_1 = T_1,  Omega_k = sum_{j<=k} T_j E_{k-j+1},  E_m = sum_q w_q D_m^(q).
+//   The GPU work is therefore the nested prefix totals T_1..T_n: n-1 products
+//   per sample instead of Q(n-1).
+//
+//   The sample axis is cut into chunks [b_c, e_c] (e_c = b_{c+1}, b_c a
+//   multiple of 4 so every rule block lies inside one chunk).  With the
+//   chunk's zero-carry local prefixes L_j, Chen's identity gives
+//       P_j[i] = sum_{m=0..j} L_{j-m}[i] pi_m     (pi_0 = 1, L_0 = 1)
+//   so chunks run in parallel and a scan over chunk summaries
+//   Lambda^c_j = L_j[e_c] carries pi (FP64) from chunk to chunk.  The adjoint
+//   runs the same structure backwards: a reverse scan of Lambda^T gives the
+//   cotangent rho on each chunk's end state, and each chunk then replays its
+//   forward (from the checkpoint pi^c) and its reverse locally.
+//
+// SpaceCurve data (a 3-vector f padded to (0, f), src/composer/backends.hpp:
+// 253-301) uses the reference product c = (a.b, -b0 a + a x b)
+// (src/linalg/spacecurve.hpp:8-18), which equals -qmul(a, b) for the
+// associative product qmul(a, b) = b (x) a (Hamilton).  With the level
+// variables scaled by (-1)^(k-1) the recursion becomes the same associative
+// recursion under qmul; outputs, cotangents and carries pick up the signs
+// (-1)^(k-1) (Omega_k) and (-1)^k (carry P_k).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mgb {
+
+enum Kind : int { KIND_MATRIX = 0, KIND_SC = 1 };
+enum Rule : int { R_BOOLE = 0, R_SIMPSON = 1, R_TRAP = 2, R_RIEMANN = 3 };
+enum OpKind : int { OP_ONE = 0, OP_MANY = 1, OP_SUM = 2 };
+
+// Per-instance descriptor, resident in device memory for the duration of a
+// call.  Level j (1..n) of an n*m block sits at offset (j-1)*m.
+struct InstDev {
+    const void* A;     // (S, d, d) or (S, 3), problem dtype
+    void* out;         // forward output, problem dtype (nullable in VJP runs)
+    void* carry;       // reference-format carry (nullable)
+    const void* cot;   // VJP cotangent (nullable in forward runs)
+    void* dA;          // VJP output (nullable in forward runs)
+    double* pi;        // (C+1) * n*m  : chunk start states, pi[C] = totals T
+    double* lam;       // C * n*m      : chunk transfer Lambda^c
+    double* rho;       // C * n*m      : cotangent on chunk c's end state
+    double* dq;        // Q * n*m      : D_k^(q), k = 1..n
+    double* ee;        // n*m          : E_k
+    double* tau;       // n*m          : cotangent on T_k
+    double* ob;        // n*m          : Omega / Omega-bar scratch
+    double* eb;        // n*m          : E-bar scratch
+    double* db;        // n*m          : D-bar scratch
+    const double* glw; // Q weights on [0, 1]
+    const double* glx; // Q nodes on [0, 1]
+    double dt;
+    int64_t S;
+    int32_t d, m, n, C, Q, K, op;
+    int32_t pad_;
+};
+
+// Chunk c of an instance: samples [b, e], e = min(b + K, S - 1).
+struct ChunkRef {
+    int32_t inst;
+    int32_t chunk;
+};
+
+// ---------------------------------------------------------------------
+// Input / output element access (problem dtype -> compute type T)
+// ---------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T load_in(const void* p, int64_t idx, bool f64) {
+    return f64 ? (T)__ldg(static_cast<const double*>(p) + idx) : (T)__ldg(static_cast<const float*>(p) + idx);
+}
+template <class T>
+__device__ __forceinline__ void store_out(void* p, int64_t idx, T v, bool f64) {
+    if (f64) static_cast<double*>(p)[idx] = (double)v;
+    else static_cast<float*>(p)[idx] = (float)v;
+}
+template <class T>
+__device__ __forceinline__ void atomic_add_out(void* p, int64_t idx, T v, bool f64) {
+    if (f64) atomicAdd(static_cast<double*>(p) + idx, (double)v);
+    else atomicAdd(static_cast<float*>(p) + idx, (float)v);
+}
+
+// Sample i, element el of the algebra element (m = d*d, or 4 for
+// SpaceCurve where component 0 is the zero padding).
+template <class T, int KIND>
+__device__ __forceinline__ T load_sample(const void* A, int64_t i, int el, int m, bool f64) {
+    if (KIND == KIND_SC) return el == 0 ? T(0) : load_in<T>(A, i * 3 + (el - 1), f64);
+    return load_in<T>(A, i * (int64_t)m + el, f64);
+}
+
+// ---------------------------------------------------------------------
+// Algebra: one output element of the products used by the recursion.
+//   mul(a, b)      : level product a (x) b
+//   adjL(a, g)[X]  : d<g, a (x) X>/dX   (cotangent to the right factor)
+//   adjR(g, b)[X]  : d<g, X (x) b>/dX   (cotangent to the left factor)
+// Operands may be of different storage types; accumulation is in T.
+// ---------------------------------------------------------------------
+template <class T, int KIND>
+struct Alg;
+
+template <class T>
+struct Alg<T, KIND_MATRIX> {
+    __device__ __forceinline__ static T one(int d, int el) { return (el / d == el % d) ? T(1) : T(0); }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T mul(const PA* a, const PB* b, int d, int el) {
+        const int r = el / d, c = el - r * d;
+        T s = T(0);
+        for (int k = 0; k < d; ++k) s += (T)a[r * d + k] * (T)b[k * d + c];
+        return s;
+    }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T adjL(const PA* a, const PB* g, int d, int el) {
+        const int r = el / d, c = el - r * d;
+        T s = T(0);
+        for (int k = 0; k < d; ++k) s += (T)a[k * d + r] * (T)g[k * d + c];
+        return s;
+    }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T adjR(const PA* g, const PB* b, int d, int el) {
+        const int r = el / d, c = el - r * d;
+        T s = T(0);
+        for (int k = 0; k < d; ++k) s += (T)g[r * d + k] * (T)b[c * d + k];
+        return s;
+    }
+};
+
+// qmul(a, b) = b (x) a (Hamilton).
+template <class T>
+struct Alg<T, KIND_SC> {
+    __device__ __forceinline__ static T one(int, int el) { return el == 0 ? T(1) : T(0); }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T mul(const PA* pa, const PB* pb, int, int el) {
+        const T a0 = (T)pa[0], a1 = (T)pa[1], a2 = (T)pa[2], a3 = (T)pa[3];
+        const T b0 = (T)pb[0], b1 = (T)pb[1], b2 = (T)pb[2], b3 = (T)pb[3];
+        switch (el) {
+            case 0: return b0 * a0 - b1 * a1 - b2 * a2 - b3 * a3;
+            case 1: return b0 * a1 + b1 * a0 + b2 * a3 - b3 * a2;
+            case 2: return b0 * a2 - b1 * a3 + b2 * a0 + b3 * a1;
+            default: return b0 * a3 + b1 * a2 - b2 * a1 + b3 * a0;
+        }
+    }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T adjL(const PA* pa, const PB* pg, int, int el) {
+        const T a0 = (T)pa[0], a1 = (T)pa[1], a2 = (T)pa[2], a3 = (T)pa[3];
+        const T g0 = (T)pg[0], g1 = (T)pg[1], g2 = (T)pg[2], g3 = (T)pg[3];
+        switch (el) {
+            case 0: return a0 * g0 + a1 * g1 + a2 * g2 + a3 * g3;
+            case 1: return -a1 * g0 + a0 * g1 - a3 * g2 + a2 * g3;
+            case 2: return -a2 * g0 + a3 * g1 + a0 * g2 - a1 * g3;
+            default: return -a3 * g0 - a2 * g1 + a1 * g2 + a0 * g3;
+        }
+    }
+    template <class PA, class PB>
+    __device__ __forceinline__ static T adjR(const PA* pg, const PB* pb, int, int el) {
+        const T p0 = (T)pb[0], p1 = (T)pb[1], p2 = (T)pb[2], p3 = (T)pb[3];
+        const T g0 = (T)pg[0], g1 = (T)pg[1], g2 = (T)pg[2], g3 = (T)pg[3];
+        switch (el) {
+            case 0: return p0 * g0 + p1 * g1 + p2 * g2 + p3 * g3;
+            case 1: return -p1 * g0 + p0 * g1 + p3 * g2 - p2 * g3;
+            case 2: return -p2 * g0 - p3 * g1 + p0 * g2 + p1 * g3;
+            default: return -p3 * g0 + p2 * g1 - p1 * g2 + p0 * g3;
+        }
+    }
+};
+
+// ---------------------------------------------------------------------
+// Block rules as streaming state machines over one element.
+// Position li is the sample index relative to the chunk start b (b is a
+// multiple of 4), so li & 3 / li & 1 give the place inside a Boole block /
+// Simpson pair.  Coefficients follow the reference's prefix rules:
+//   Boole     src/integration/boole.hpp:24-74
+//   Simpson   src/integration/simpson.hpp:24-58
+//   Trapezoid src/integration/trapezoid.hpp:23-33 (textbook increments; the
+//             reference's differencing recurrence equals them up to rounding)
+//   Riemann   src/integration/default.hpp:23-26 (inclusive: P_0 = dt f_0)
+// ---------------------------------------------------------------------
+template <class T>
+struct RuleCoef {
+    T h, t3, c38, c98, c4_3, b14, b64, b24, dt;
+    __device__ __forceinline__ explicit RuleCoef(double dtd)
+        : h((T)(dtd / 2)), t3((T)(dtd / 3)), c38((T)(3 * dtd / 8)), c98((T)(9 * dtd / 8)),
+          c4_3((T)(4 * dtd / 3)), b14((T)(14 * dtd / 45)), b64((T)(64 * dtd / 45)), b24((T)(24 * dtd / 45)),
+          dt((T)dtd) {}
+};
+
+// A chunk carry (FP64 on the host side) as an unevaluated sum hi + lo in the
+// compute type: exact for double, ~2x float precision for float.  Running
+// prefix states stay LOCAL to the chunk (they start at zero) and the carry is
+// added only when a value is emitted, so FP32 rounding in the mixed form
+// scales with the chunk's own increments, not with the carried total.
+template <class T>
+struct Carry {
+    T hi, lo;
+};
+template <class T>
+__device__ __forceinline__ Carry<T> split_carry(double v) {
+    Carry<T> c;
+    c.hi = (T)v;
+    c.lo = (T)(v - (double)c.hi);
+    return c;
+}
+template <class T>
+__device__ __forceinline__ T add_carry(T local, const Carry<T>& c) {
+    return (local + c.lo) + c.hi;
+}
+
+template <class T>
+struct FwdState {
+    T base, f0, f1, f2, f3;  // base: local prefix at the last anchor
+};
+
+// Returns P at position li (carry included) given f at li; updates the state.
+template <class T, int RULE>
+__device__ __forceinline__ T fwd_step(FwdState<T>& s, T f, int li, const RuleCoef<T>& k, const Carry<T>& cy) {
+    if (RULE == R_BOOLE) {
+        switch (li & 3) {
+            case 1: s.f1 = f; return add_carry(f * k.h + s.f0 * k.h + s.base, cy);
+            case 2: s.f2 = f; return add_carry(f * k.t3 + s.f0 * k.t3 + s.f1 * k.c4_3 + s.base, cy);
+            case 3: s.f3 = f; return add_carry(f * k.c38 + s.f0 * k.c38 + s.f1 * k.c98 + s.f2 * k.c98 + s.base, cy);
+            default: {
+                T P = f * k.b14 + s.f0 * k.b14 + s.f1 * k.b64 + s.f2 * k.b24 + s.f3 * k.b64 + s.base;
+                s.base = P;
+                s.f0 = f;
+                return add_carry(P, cy);
+            }
+        }
+    } else if (RULE == R_SIMPSON) {
+        if (li & 1) {
+            s.f1 = f;
+            return add_carry(f * k.h + s.f0 * k.h + s.base, cy);
+        }
+        T P = f * k.t3 + s.f0 * k.t3 + s.f1 * (T(4) * k.t3) + s.base;
+        s.base = P;
+        s.f0 = f;
+        return add_carry(P, cy);
+    } else if (RULE == R_TRAP) {
+        T P = f * k.h + s.f0 * k.h + s.base;
+        s.base = P;
+        s.f0 = f;
+        return add_carry(P, cy);
+    } else {
+        T P = f * k.dt + s.base;
+        s.base = P;
+        return add_carry(P, cy);
+    }
+}
+
+// Adjoint of the block rules, processing positions from the chunk end
+// downwards.  Rb: LOCAL cotangent on the current anchor prefix from later
+// samples of the chunk (the cotangent rho from beyond the chunk is the carry
+// cy, added where totals are used); pend: cotangent on the anchor's f from
+// its use as the first sample of the later block.  Input H: local cotangent
+// on P[li]; returns the cotangent on f[li].
+template <class T>
+struct RevState {
+    T Rb, pend, R4l, R4, H2, H3;
+};
+
+template <class T, int RULE>
+__device__ __forceinline__ T rev_step(RevState<T>& s, T H, int li, const RuleCoef<T>& k, const Carry<T>& cy) {
+    if (RULE == R_BOOLE) {
+        switch (li & 3) {
+            case 0: {
+                s.R4l = H + s.Rb;
+                s.R4 = add_carry(s.R4l, cy);
+                return s.R4 * k.b14 + s.pend;
+            }
+            case 3: s.H3 = H; return H * k.c38 + s.R4 * k.b64;
+            case 2: s.H2 = H; return H * k.t3 + s.H3 * k.c98 + s.R4 * k.b24;
+            default: {
+                T G = H * k.h + s.H2 * k.c4_3 + s.H3 * k.c98 + s.R4 * k.b64;
+                s.pend = H * k.h + s.H2 * k.t3 + s.H3 * k.c38 + s.R4 * k.b14;
+                s.Rb = H + s.H2 + s.H3 + s.R4l;
+                return G;
+            }
+        }
+    } else if (RULE == R_SIMPSON) {
+        if ((li & 1) == 0) {
+            s.R4l = H + s.Rb;
+            s.R4 = add_carry(s.R4l, cy);
+            return s.R4 * k.t3 + s.pend;
+        }
+        T G = H * k.h + s.R4 * (T(4) * k.t3);
+        s.pend = H * k.h + s.R4 * k.t3;
+        s.Rb = H + s.R4l;
+        return G;
+    } else if (RULE == R_TRAP) {
+        T Rl = H + s.Rb;
+        T Rt = add_carry(Rl, cy);
+        T G = Rt * k.h + s.pend;
+        s.Rb = Rl;
+        s.pend = Rt * k.h;
+        return G;
+    } else {
+        T Rl = H + s.Rb;
+        s.Rb = Rl;
+        return add_carry(Rl, cy) * k.dt;
+    }
+}
+
+}  // namespace mgb

@@ -1,0 +1,393 @@
+// Shape-specialised chunk kernel for the mixed form (FP32 products, FP64
+// carries) at d = 16 and d = 32: one CTA per chunk, samples processed in
+// groups of G (G = 256 / (d/4)^2, so every thread owns one 4x4 output tile
+// of one sample), all Magnus levels per group, per-level prefix state in
+// shared memory.
+//
+// Per group and level: a prefix pass (thread per element, FP32 local
+// accumulators, FP64 chunk carry added at emission) and a batched
+// 4x4-register-tiled product pass with operands in shared memory:
+//   forward  W = A P        A^T and P staged with a 16-byte row pitch (float4 loads)
+//   adjoint  H = A^T G      A (float4 rows) x G (odd pitch, conflict-free scalars)
+//            dA += G P^T    G (odd pitch) x P^T (float4 rows, from the tape)
+// The VJP replays the chunk forward from its checkpoint, writing the prefix
+// values of levels 1..n-1 to a per-CTA tape in global memory, then runs the
+// adjoint over the groups in reverse order with dA accumulated in registers.
+#include <cstdint>
+#include <vector>
+
+#include "mgb_common.cuh"
+#include "mgb_tuned.h"
+
+namespace mgb {
+namespace {
+
+constexpr int TNT = 256;
+
+template <int D>
+struct TileCfg {
+    static constexpr int m = D * D;
+    static constexpr int TPS = (D / 4) * (D / 4);  // threads per sample
+    static constexpr int G = TNT / TPS;           // samples per group
+    static constexpr int P4 = D + 4;              // 16-byte aligned pitch
+    static constexpr int P1 = D + 1;              // odd pitch (column reads)
+    static constexpr int EPT = m / TNT;           // prefix elements per thread
+    static constexpr int OPND = (3 * G * D * P4 > 2 * G * D * P4 + 2 * G * D * P1) ? 3 * G * D * P4
+                                                                                   : 2 * G * D * P4 + 2 * G * D * P1;
+    static_assert(G * TPS == TNT, "tile mapping");
+    static_assert(EPT >= 1 && EPT * TNT == m, "prefix mapping");
+};
+
+// acc += X Y with X given transposed (XT[k][r], pitch px) and Y row-major
+// (pitch py); both 16-byte aligned rows.
+template <int D>
+__device__ __forceinline__ void mma_tv(float (&acc)[4][4], const float* __restrict__ XT, int px,
+                                       const float* __restrict__ Y, int py, int r0, int c0) {
+#pragma unroll 8
+    for (int k = 0; k < D; ++k) {
+        const float4 a = *reinterpret_cast<const float4*>(XT + k * px + r0);
+        const float4 b = *reinterpret_cast<const float4*>(Y + k * py + c0);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[t][u] = fmaf(av[t], bv[u], acc[t][u]);
+    }
+}
+
+// acc += A^T G : A row-major (pitch P4, float4), G row-major odd pitch P1.
+template <int D>
+__device__ __forceinline__ void mma_adjL(float (&acc)[4][4], const float* __restrict__ A,
+                                         const float* __restrict__ G, int r0, int c0) {
+    constexpr int P4 = D + 4, P1 = D + 1;
+#pragma unroll 8
+    for (int k = 0; k < D; ++k) {
+        const float4 a = *reinterpret_cast<const float4*>(A + k * P4 + r0);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        float bv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) bv[u] = G[k * P1 + c0 + u];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[t][u] = fmaf(av[t], bv[u], acc[t][u]);
+    }
+}
+
+// acc += G P^T : G row-major odd pitch P1 (column reads), P^T row-major P4.
+template <int D>
+__device__ __forceinline__ void mma_adjR(float (&acc)[4][4], const float* __restrict__ G,
+                                         const float* __restrict__ PT, int r0, int c0) {
+    constexpr int P4 = D + 4, P1 = D + 1;
+#pragma unroll 8
+    for (int k = 0; k < D; ++k) {
+        float av[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) av[t] = G[(r0 + t) * P1 + k];
+        const float4 b = *reinterpret_cast<const float4*>(PT + k * P4 + c0);
+        const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[t][u] = fmaf(av[t], bv[u], acc[t][u]);
+    }
+}
+
+template <int D, int RULE, int MODE>
+__global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work,
+                                                 int64_t nwork, float* __restrict__ scratch, int64_t slot_elems) {
+    using Cf = TileCfg<D>;
+    constexpr int m = Cf::m, G = Cf::G, P4 = Cf::P4, P1 = Cf::P1, TPS = Cf::TPS, EPT = Cf::EPT;
+    extern __shared__ __align__(16) float sm[];
+    float* const sAT = sm;               // forward: A^T   [G][D][P4]
+    float* const sP = sAT + G * D * P4;  // forward: P     [G][D][P4]
+    float* const sF = sP + G * D * P4;   // forward: f     [G][D][P4]
+    float* const sA = sm;                // reverse: A     [G][D][P4]
+    float* const sPT = sA + G * D * P4;  // reverse: P^T   [G][D][P4]
+    float* const sG = sPT + G * D * P4;  // reverse: G     [G][D][P1]
+    float* const sH = sG + G * D * P1;   // reverse: H     [G][D][P1]
+    float* const st = sm + Cf::OPND;     // state [n][2][m]
+    float* const tape = scratch + (int64_t)blockIdx.x * slot_elems;
+
+    const int tid = threadIdx.x;
+    const int tl = tid / TPS, tu = tid % TPS;
+    const int r0 = (tu / (D / 4)) * 4, c0 = (tu % (D / 4)) * 4;
+
+    for (int64_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const ChunkRef wk = work[w];
+        const InstDev& I = insts[wk.inst];
+        const int c = wk.chunk, n = I.n;
+        const int64_t b = (int64_t)c * I.K;
+        const int64_t e = (b + I.K < I.S - 1) ? b + I.K : I.S - 1;
+        const int Kp = (int)(e - b), L = Kp + 1;
+        const bool riem0 = (RULE == R_RIEMANN) && c == 0;
+        const int first = riem0 ? 0 : 1;
+        const int64_t nm = (int64_t)n * m;
+        const RuleCoef<float> kc(I.dt);
+        const double* pic = I.pi + (int64_t)c * nm;
+        const float* Ag = static_cast<const float*>(I.A) + b * m;
+        const int NLf = (MODE == MODE_LOCAL) ? n : n - 1;  // levels with a forward prefix
+
+        // ---------------- forward state at the chunk start ----------------
+        for (int j = 1; j <= NLf; ++j)
+            for (int q = 0; q < EPT; ++q) {
+                const int el = tid + q * TNT;
+                st[(j - 1) * 2 * m + el] = 0.f;
+                st[(j - 1) * 2 * m + m + el] = (j == 1) ? __ldg(Ag + el) : 0.f;
+            }
+        if (MODE == MODE_VJP && !riem0 && NLf >= 2) {
+            // f0_j = A[b] P_{j-1}[b] = A[b] pi_{j-1} for j = 2..NLf
+            for (int el = tid; el < m; el += TNT) sAT[(el % D) * P4 + el / D] = __ldg(Ag + el);
+            for (int j0 = 2; j0 <= NLf; j0 += G) {
+                for (int idx = tid; idx < G * m; idx += TNT) {
+                    const int l = idx / m, el = idx % m;
+                    if (j0 + l <= NLf) sP[l * D * P4 + (el / D) * P4 + el % D] = (float)pic[(int64_t)(j0 + l - 2) * m + el];
+                }
+                __syncthreads();
+                if (j0 + tl <= NLf) {
+                    float acc[4][4] = {};
+                    mma_tv<D>(acc, sAT, P4, sP + tl * D * P4, P4, r0, c0);
+                    float* f0 = st + (j0 + tl - 1) * 2 * m + m;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) f0[(r0 + t) * D + c0 + u] = acc[t][u];
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+
+        // ---------------- forward over the groups ----------------
+        for (int li0 = first; li0 <= Kp; li0 += G) {
+            const int ge = min(G, Kp - li0 + 1);
+            {
+                const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
+                for (int i4 = tid; i4 < ge * m / 4; i4 += TNT) {
+                    const float4 v = __ldg(src + i4);
+                    const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                    *reinterpret_cast<float4*>(sF + l * D * P4 + r * P4 + cc) = v;
+                    float* at = sAT + l * D * P4 + r;
+                    at[(cc + 0) * P4] = v.x;
+                    at[(cc + 1) * P4] = v.y;
+                    at[(cc + 2) * P4] = v.z;
+                    at[(cc + 3) * P4] = v.w;
+                }
+            }
+            __syncthreads();
+            for (int j = 1; j <= NLf; ++j) {
+#pragma unroll
+                for (int q = 0; q < EPT; ++q) {
+                    const int el = tid + q * TNT, r = el / D, cc = el % D;
+                    const Carry<float> cy =
+                        split_carry<float>((MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el]);
+                    float* sj = st + (j - 1) * 2 * m;
+                    FwdState<float> s;
+                    s.base = sj[el];
+                    s.f0 = sj[m + el];
+                    s.f1 = s.f2 = s.f3 = 0.f;
+                    for (int l = 0; l < ge; ++l) {
+                        const float P = fwd_step<float, RULE>(s, sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
+                        sP[l * D * P4 + r * P4 + cc] = P;
+                        if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
+                    }
+                    sj[el] = s.base;
+                    sj[m + el] = s.f0;
+                }
+                __syncthreads();
+                if (j < NLf) {
+                    if (tl < ge) {
+                        float acc[4][4] = {};
+                        mma_tv<D>(acc, sAT + tl * D * P4, P4, sP + tl * D * P4, P4, r0, c0);
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                            *reinterpret_cast<float4*>(sF + tl * D * P4 + (r0 + t) * P4 + c0) =
+                                make_float4(acc[t][0], acc[t][1], acc[t][2], acc[t][3]);
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+
+        if (MODE == MODE_LOCAL) {
+            for (int j = 1; j <= n; ++j)
+                for (int q = 0; q < EPT; ++q) {
+                    const int el = tid + q * TNT;
+                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] = (double)st[(j - 1) * 2 * m + el];
+                }
+        }
+
+        if (MODE == MODE_VJP) {
+            __syncthreads();
+            const double* rc = I.rho + (int64_t)c * nm;
+            for (int j = 1; j <= n; ++j)
+                for (int q = 0; q < EPT; ++q) {
+                    const int el = tid + q * TNT;
+                    st[(j - 1) * 2 * m + el] = 0.f;      // Rb (local)
+                    st[(j - 1) * 2 * m + m + el] = 0.f;  // pend
+                }
+            float* dAg = static_cast<float*>(I.dA) + b * m;
+            const int last0 = first + ((Kp - first) / G) * G;
+            for (int li0 = last0; li0 >= first; li0 -= G) {
+                const int ge = min(G, Kp - li0 + 1);
+                {
+                    const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
+                    for (int i4 = tid; i4 < ge * m / 4; i4 += TNT) {
+                        const float4 v = __ldg(src + i4);
+                        const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                        *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = v;
+                    }
+                }
+                float dacc[4][4] = {};
+                for (int j = n; j >= 1; --j) {
+                    if (j < n) {
+                        const float* src = tape + ((int64_t)(j - 1) * L + li0) * m;
+                        for (int idx = tid; idx < ge * m; idx += TNT) {
+                            const int l = idx / m, el = idx % m, r = el / D, cc = el % D;
+                            sPT[l * D * P4 + cc * P4 + r] = src[idx];
+                        }
+                        __syncthreads();
+                        if (tl < ge) {
+                            float hacc[4][4] = {};
+                            mma_adjL<D>(hacc, sA + tl * D * P4, sG + tl * D * P1, r0, c0);
+                            mma_adjR<D>(dacc, sG + tl * D * P1, sPT + tl * D * P4, r0, c0);
+#pragma unroll
+                            for (int t = 0; t < 4; ++t)
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) sH[tl * D * P1 + (r0 + t) * P1 + c0 + u] = hacc[t][u];
+                        }
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int q = 0; q < EPT; ++q) {
+                        const int el = tid + q * TNT, r = el / D, cc = el % D;
+                        const Carry<float> cy = split_carry<float>(rc[(int64_t)(j - 1) * m + el]);
+                        float* sj = st + (j - 1) * 2 * m;
+                        RevState<float> s;
+                        s.Rb = sj[el];
+                        s.pend = sj[m + el];
+                        s.R4l = s.R4 = s.H2 = s.H3 = 0.f;
+                        for (int l = ge - 1; l >= 0; --l) {
+                            const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
+                            sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(s, H, li0 + l, kc, cy);
+                        }
+                        sj[el] = s.Rb;
+                        sj[m + el] = s.pend;
+                    }
+                    __syncthreads();
+                }
+                if (tl < ge) {
+                    const int li = li0 + tl;
+                    const bool shared = (li == Kp && c < I.C - 1);
+                    float* row = dAg + (int64_t)li * m;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        float v[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) v[u] = dacc[t][u] + sG[tl * D * P1 + (r0 + t) * P1 + c0 + u];
+                        float* dst = row + (r0 + t) * D + c0;
+                        if (shared) {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) atomicAdd(dst + u, v[u]);
+                        } else {
+                            *reinterpret_cast<float4*>(dst) = make_float4(v[0], v[1], v[2], v[3]);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            // chunk start sample: cotangent pend_j on this chunk's copy of
+            // W_j[b]; dA[b] += pend_1 + sum_{j<n} pend_{j+1} pi_j^T
+            if (!riem0 && RULE != R_RIEMANN) {
+                float bacc[4][4] = {};
+                for (int j = 1; j < n; ++j) {
+                    for (int el = tid; el < m; el += TNT) {
+                        const int r = el / D, cc = el % D;
+                        sG[r * P1 + cc] = st[j * 2 * m + m + el];
+                        sPT[cc * P4 + r] = (float)pic[(int64_t)(j - 1) * m + el];
+                    }
+                    __syncthreads();
+                    if (tl == 0) mma_adjR<D>(bacc, sG, sPT, r0, c0);
+                    __syncthreads();
+                }
+                if (tl == 0) {
+                    float* row = dAg;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int el = (r0 + t) * D + c0 + u;
+                            const float v = bacc[t][u] + st[m + el];
+                            if (c > 0) atomicAdd(row + el, v);
+                            else row[el] = v;
+                        }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int D>
+size_t tile_smem_bytes(int nmax) {
+    return ((size_t)TileCfg<D>::OPND + 2 * (size_t)nmax * TileCfg<D>::m) * sizeof(float);
+}
+
+template <int D, int RULE, int MODE>
+cudaError_t launch_tile_t(const LaunchArgs& a, int nmax, int grid) {
+    const size_t smem = tile_smem_bytes<D>(nmax);
+    cudaError_t e = cudaFuncSetAttribute(k_tile<D, RULE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_tile<D, RULE, MODE><<<grid, TNT, smem, a.stream>>>(a.insts, a.work, a.nwork, static_cast<float*>(a.scratch),
+                                                        a.slot_elems);
+    return cudaGetLastError();
+}
+
+template <int D, int MODE>
+cudaError_t launch_tile_r(int rule, const LaunchArgs& a, int nmax, int grid) {
+    switch (rule) {
+        case R_BOOLE: return launch_tile_t<D, R_BOOLE, MODE>(a, nmax, grid);
+        case R_SIMPSON: return launch_tile_t<D, R_SIMPSON, MODE>(a, nmax, grid);
+        case R_TRAP: return launch_tile_t<D, R_TRAP, MODE>(a, nmax, grid);
+        default: return launch_tile_t<D, R_RIEMANN, MODE>(a, nmax, grid);
+    }
+}
+
+}  // namespace
+
+TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi) {
+    TunedChoice tc;
+    (void)rule;
+    if (plain || f64io || kind != KIND_MATRIX || hi.empty()) return tc;
+    if (mode != MODE_LOCAL && mode != MODE_VJP) return tc;
+    const int D = hi[0].d;
+    if (D != 16 && D != 32) return tc;
+    int nmax = 0;
+    for (const InstDev& I : hi) {
+        if (I.d != D || I.n < 1) return tc;
+        if (reinterpret_cast<uintptr_t>(I.A) % 16 != 0) return tc;
+        if (mode == MODE_VJP && reinterpret_cast<uintptr_t>(I.dA) % 16 != 0) return tc;
+        nmax = I.n > nmax ? I.n : nmax;
+    }
+    const size_t smem = D == 32 ? tile_smem_bytes<32>(nmax) : tile_smem_bytes<16>(nmax);
+    if (smem > 227 * 1024) return tc;
+    tc.use = true;
+    tc.family = 2;
+    tc.D = D;
+    tc.nmax = nmax;
+    tc.ctas_per_sm = smem <= 113 * 1024 ? 2 : 1;
+    return tc;
+}
+
+cudaError_t launch_tuned(const TunedChoice& tc, bool, int, int rule, int mode, const LaunchArgs& a, int sms) {
+    int grid = (int)std::min<int64_t>(a.grid, (int64_t)sms * tc.ctas_per_sm);
+    if (grid < 1) grid = 1;
+    if (tc.D == 32)
+        return mode == MODE_LOCAL ? launch_tile_r<32, MODE_LOCAL>(rule, a, tc.nmax, grid)
+                                  : launch_tile_r<32, MODE_VJP>(rule, a, tc.nmax, grid);
+    return mode == MODE_LOCAL ? launch_tile_r<16, MODE_LOCAL>(rule, a, tc.nmax, grid)
+                              : launch_tile_r<16, MODE_VJP>(rule, a, tc.nmax, grid);
+}
+
+}  // namespace mgb

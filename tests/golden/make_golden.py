@@ -1,0 +1,141 @@
+"""Generates the golden fixtures in this directory from the reference
+implementation itself (s-cavalier/magnus-dp compiled from its own sources by
+oracle/build_ref.sh into oracle/_ref/).
+
+Run from the repository root:   python tests/golden/make_golden.py
+
+Every case stores its inputs and the reference's outputs, computed with the
+serial Gauss-Legendre backend and the Fixed2 / Manual / SpaceCurve policies
+(exact reference arithmetic; the Blas policy is MKL-dependent and not used).
+The fixtures are read by tests/ only; nothing at run time needs the
+reference.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+sys.path.insert(0, os.path.join(ROOT, "magnus-dp_gb300"))
+
+import magnus  # noqa: E402  (the reference, from oracle/_ref)
+from magnus_gb300 import workloads  # noqa: E402
+
+core = magnus._core
+
+
+def backend(d):
+    return "Fixed2" if d == 2 else "Manual"
+
+
+def small_cases():
+    rng = np.random.default_rng(1234)
+    cases = {}
+    idx = 0
+    for integ, S in [("Boole", 17), ("Simpson", 13), ("Trapezoid", 11), ("Riemann", 10)]:
+        for d in (2, 3, 5):
+            A = rng.standard_normal((S, d, d)) / np.sqrt(d)
+            for n in (1, 2, 4, 6):
+                for op in ("one", "many", "sum"):
+                    key = f"m{idx:03d}"
+                    idx += 1
+                    out = core.compute(n, A, 0.0, 1.3, op=op, matrix_backend=backend(d), integrator=integ,
+                                       gl_backend="serial")
+                    cot = rng.standard_normal(out.shape)
+                    dA = core.compute_vjp(n, A, cot, t0=0.0, tf=1.3, op=op, matrix_backend=backend(d),
+                                          integrator=integ)
+                    cases[key] = dict(kind="matrix", integrator=integ, op=op, n=n, t0=0.0, tf=1.3, A=A, out=out,
+                                      cot=cot, dA=dA)
+                    if n == 4 and op == "sum":
+                        _, carry = core.compute(n, A, 0.0, 1.3, op=op, matrix_backend=backend(d), integrator=integ,
+                                                gl_backend="serial", record_vjp=True)
+                        cases[key]["carry"] = carry
+        F = rng.standard_normal((S, 3))
+        for n in (1, 2, 4, 6):
+            for op in ("one", "many", "sum"):
+                key = f"s{idx:03d}"
+                idx += 1
+                out = core.compute_sc(n, F, 0.0, 2.0, op=op, integrator=integ, gl_backend="serial")
+                cot = rng.standard_normal(out.shape)
+                dA = core.compute_sc_vjp(n, F, cot, t0=0.0, tf=2.0, op=op, integrator=integ)
+                cases[key] = dict(kind="spacecurve", integrator=integ, op=op, n=n, t0=0.0, tf=2.0, A=F, out=out,
+                                  cot=cot, dA=dA)
+                if n == 4 and op == "many":
+                    _, carry = core.compute_sc(n, F, 0.0, 2.0, op=op, integrator=integ, gl_backend="serial",
+                                               record_vjp=True)
+                    cases[key]["carry"] = carry
+    return cases
+
+
+def medium_cases():
+    """Multi-chunk sizes (the engine's default chunk is 256 samples; tests
+    also force small chunks)."""
+    rng = np.random.default_rng(99)
+    cases = {}
+    for key, (integ, S, d, n, op) in {
+        "md16": ("Boole", 261, 16, 5, "sum"),
+        "md8s": ("Simpson", 301, 8, 4, "many"),
+        "md4t": ("Trapezoid", 257, 4, 3, "one"),
+        "md3r": ("Riemann", 300, 3, 6, "many"),
+    }.items():
+        A = rng.standard_normal((S, d, d)) / np.sqrt(d)
+        out = core.compute(n, A, 0.0, 1.0, op=op, matrix_backend=backend(d), integrator=integ, gl_backend="serial")
+        cot = rng.standard_normal(out.shape)
+        dA = core.compute_vjp(n, A, cot, t0=0.0, tf=1.0, op=op, matrix_backend=backend(d), integrator=integ)
+        cases[key] = dict(kind="matrix", integrator=integ, op=op, n=n, t0=0.0, tf=1.0, A=A, out=out, cot=cot, dA=dA)
+    F = workloads.config1_samples_np(*workloads.config1_coeffs(seed=1, batch=1), samples=1025, dtype=np.float64)[0]
+    out = core.compute_sc(6, F, 0.0, 2.0, op="many", integrator="Simpson", gl_backend="serial")
+    cot = rng.standard_normal(out.shape)
+    dA = core.compute_sc_vjp(6, F, cot, t0=0.0, tf=2.0, op="many", integrator="Simpson")
+    cases["mdsc"] = dict(kind="spacecurve", integrator="Simpson", op="many", n=6, t0=0.0, tf=2.0, A=F, out=out,
+                         cot=cot, dA=dA)
+    return cases
+
+
+def config0_cases():
+    A = workloads.config0_samples(seed=0)
+    cases = {}
+    for op in ("sum", "many"):
+        out = core.compute(4, A, 0.0, 1.0, op=op, matrix_backend="Fixed2", integrator="Boole", gl_backend="serial")
+        cases[f"cfg0_{op}"] = dict(kind="matrix", integrator="Boole", op=op, n=4, t0=0.0, tf=1.0, A=A, out=out)
+    return cases
+
+
+def float32_cases():
+    """Reference float32 runs next to the float64 run on the upcast input
+    (the float64 run is the accuracy oracle for float32 data)."""
+    rng = np.random.default_rng(7)
+    A32 = (rng.standard_normal((129, 4, 4)) / 2).astype(np.float32)
+    cases = {}
+    out32 = core.compute(5, A32, 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole", gl_backend="serial")
+    out64 = core.compute(5, A32.astype(np.float64), 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole",
+                         gl_backend="serial")
+    cases["f32"] = dict(kind="matrix", integrator="Boole", op="many", n=5, t0=0.0, tf=1.0, A=A32, out=out32,
+                        out64=out64)
+    return cases
+
+
+def save(name, cases):
+    flat = {}
+    for key, c in cases.items():
+        for field, value in c.items():
+            flat[f"{key}/{field}"] = np.asarray(value)
+    np.savez_compressed(os.path.join(HERE, name), **flat)
+
+
+def main():
+    save("small.npz", small_cases())
+    save("medium.npz", medium_cases())
+    save("config0.npz", config0_cases())
+    save("float32.npz", float32_cases())
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()
