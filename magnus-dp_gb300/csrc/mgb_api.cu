@@ -2,6 +2,7 @@
 // the reference's error contract, call planning, a stream-ordered workspace,
 // and the kernel launch sequences for forward and VJP.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
@@ -166,7 +167,18 @@ mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
 }
 
 size_t ckpt_doubles(const mgb_problem& p, const Derived& dv) { return (size_t)(2 * dv.C + 1) * dv.nm; }
-size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + (size_t)dv.Q * dv.nm + 5 * (size_t)dv.nm; }
+size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + (size_t)dv.Q * dv.nm + 6 * (size_t)dv.nm; }
+
+// Step used inside the chunk kernels (see InstDev::dt_k): the plain form
+// integrates with dt itself; the mixed form with u * 2^p, u the rule's
+// coefficient denominator, so that all FP32 rule weights are exact.
+double kernel_step(const mgb_problem& p, double dt) {
+    if (p.precision == MGB_PRECISION_PLAIN || !(dt > 0.0) || !std::isfinite(dt)) return dt;
+    const double u = p.integrator == MGB_INTEGRATOR_BOOLE ? 90.0
+                   : p.integrator == MGB_INTEGRATOR_SIMPSON ? 6.0
+                   : p.integrator == MGB_INTEGRATOR_TRAPEZOID ? 2.0 : 1.0;
+    return u * std::exp2(std::round(std::log2(dt / u)));
+}
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
@@ -241,7 +253,7 @@ mgb_status run(const Call& call) {
         if (!user_ck) ck_doubles += ckpt_doubles(p, dv[i]);
         wsd += ws_doubles(dv[i]);
         const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
-        slot_elems = std::max<int64_t>(slot_elems, (int64_t)(p.n + 4) * L * dv[i].m);
+        slot_elems = std::max<int64_t>(slot_elems, (int64_t)(p.n + 4) * L * dv[i].m + 3 * (int64_t)p.n * dv[i].m);
         if (!call.vjp && call.carry && call.carry[i]) any_carry = true;
     }
     if (nwork > (size_t)std::numeric_limits<int32_t>::max()) return fail(MGB_ERR_INVALID_ARGUMENT, "input shape is too large");
@@ -305,6 +317,7 @@ mgb_status run(const Call& call) {
         I.ob = w; w += v.nm;
         I.eb = w; w += v.nm;
         I.db = w; w += v.nm;
+        I.tt = w; w += v.nm;
         double* g = reinterpret_cast<double*>(base + off_gl) + glpos;
         const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
         for (int q = 0; q < v.Q; ++q) {
@@ -315,6 +328,8 @@ mgb_status run(const Call& call) {
         I.glx = g + v.Q;
         glpos += 2 * (size_t)v.Q;
         I.dt = (p.tf - p.t0) / (double)(p.samples - 1);
+        I.dt_k = kernel_step(p, I.dt);
+        I.sig = (I.dt_k != 0.0) ? I.dt / I.dt_k : 1.0;
         I.S = (int64_t)p.samples;
         I.d = (p.kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p.dim;
         I.m = v.m;
@@ -352,14 +367,14 @@ mgb_status run(const Call& call) {
     if (!call.vjp || !all_ck_in) {
         (void)need_fwd_scan;
         MGB_CUDA_TRY(timed("chunk_local", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_LOCAL, la, hi, di.sms); }));
-        MGB_CUDA_TRY(timed("scan", call.stream, [&] { return launch_small(plain, kind, SMALL_SCAN, d_inst, cnt, f64io, 0, call.stream); }));
+        MGB_CUDA_TRY(timed("scan", call.stream, [&] { return launch_small(true, kind, SMALL_SCAN, d_inst, cnt, f64io, 0, call.stream); }));
     }
     MGB_CUDA_TRY(timed("fin_fwd", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_FWD, d_inst, cnt, f64io, call.vjp ? 0 : 1, call.stream); }));
     if (!call.vjp) {
         if (any_carry) MGB_CUDA_TRY(timed("chunk_carry", call.stream, [&] { return launch_generic_chunk(plain, kind, rule, MODE_CARRY, la); }));
     } else {
         MGB_CUDA_TRY(timed("fin_vjp", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_VJP, d_inst, cnt, f64io, 0, call.stream); }));
-        MGB_CUDA_TRY(timed("rscan", call.stream, [&] { return launch_small(plain, kind, SMALL_RSCAN, d_inst, cnt, f64io, 0, call.stream); }));
+        MGB_CUDA_TRY(timed("rscan", call.stream, [&] { return launch_small(true, kind, SMALL_RSCAN, d_inst, cnt, f64io, 0, call.stream); }));
         MGB_CUDA_TRY(timed("chunk_vjp", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_VJP, la, hi, di.sms); }));
     }
     return MGB_OK;

@@ -59,9 +59,17 @@ struct InstDev {
     double* ob;        // n*m          : Omega / Omega-bar scratch
     double* eb;        // n*m          : E-bar scratch
     double* db;        // n*m          : D-bar scratch
+    double* tt;        // n*m          : totals T_j = sig^j * pi[C]_j
     const double* glw; // Q weights on [0, 1]
     const double* glx; // Q nodes on [0, 1]
     double dt;
+    // The chunk kernels integrate with step dt_k and the totals are rescaled
+    // by sig^j = (dt/dt_k)^j in FP64 (prefix level j is homogeneous of degree
+    // j in the step).  Plain form: dt_k = dt, sig = 1.  Mixed form: dt_k is a
+    // power of two times the rule's coefficient denominator (90 Boole, 6
+    // Simpson, 2 Trapezoid, 1 Riemann), so every rule weight is exact in FP32.
+    double dt_k;
+    double sig;
     int64_t S;
     int32_t d, m, n, C, Q, K, op;
     int32_t pad_;
@@ -215,9 +223,33 @@ __device__ __forceinline__ T add_carry(T local, const Carry<T>& c) {
     return (local + c.lo) + c.hi;
 }
 
+// Error-free sum a + b = s + err (Knuth's TwoSum), used to carry the local
+// prefix accumulators at twice the working precision in FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
+    s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+}
+
+// acc (+ lo) += inc.  FP32: compensated, the rounding error kept in lo.
+// FP64: plain addition (lo stays 0).
+template <class T>
+__device__ __forceinline__ void acc_add(T& acc, T& lo, T inc);
+template <>
+__device__ __forceinline__ void acc_add<float>(float& acc, float& lo, float inc) {
+    float s, err;
+    two_sum(acc, inc + lo, s, err);
+    acc = s;
+    lo = err;
+}
+template <>
+__device__ __forceinline__ void acc_add<double>(double& acc, double&, double inc) {
+    acc += inc;
+}
+
 template <class T>
 struct FwdState {
-    T base, f0, f1, f2, f3;  // base: local prefix at the last anchor
+    T base, blo, f0, f1, f2, f3;  // base (+ blo): local prefix at the last anchor
 };
 
 // Returns P at position li (carry included) given f at li; updates the state.
@@ -225,46 +257,46 @@ template <class T, int RULE>
 __device__ __forceinline__ T fwd_step(FwdState<T>& s, T f, int li, const RuleCoef<T>& k, const Carry<T>& cy) {
     if (RULE == R_BOOLE) {
         switch (li & 3) {
-            case 1: s.f1 = f; return add_carry(f * k.h + s.f0 * k.h + s.base, cy);
-            case 2: s.f2 = f; return add_carry(f * k.t3 + s.f0 * k.t3 + s.f1 * k.c4_3 + s.base, cy);
-            case 3: s.f3 = f; return add_carry(f * k.c38 + s.f0 * k.c38 + s.f1 * k.c98 + s.f2 * k.c98 + s.base, cy);
+            case 1: s.f1 = f; return add_carry((f * k.h + s.f0 * k.h + s.blo) + s.base, cy);
+            case 2: s.f2 = f; return add_carry((f * k.t3 + s.f0 * k.t3 + s.f1 * k.c4_3 + s.blo) + s.base, cy);
+            case 3:
+                s.f3 = f;
+                return add_carry((f * k.c38 + s.f0 * k.c38 + s.f1 * k.c98 + s.f2 * k.c98 + s.blo) + s.base, cy);
             default: {
-                T P = f * k.b14 + s.f0 * k.b14 + s.f1 * k.b64 + s.f2 * k.b24 + s.f3 * k.b64 + s.base;
-                s.base = P;
+                const T inc = f * k.b14 + s.f0 * k.b14 + s.f1 * k.b64 + s.f2 * k.b24 + s.f3 * k.b64;
+                acc_add(s.base, s.blo, inc);
                 s.f0 = f;
-                return add_carry(P, cy);
+                return add_carry(s.base + s.blo, cy);
             }
         }
     } else if (RULE == R_SIMPSON) {
         if (li & 1) {
             s.f1 = f;
-            return add_carry(f * k.h + s.f0 * k.h + s.base, cy);
+            return add_carry((f * k.h + s.f0 * k.h + s.blo) + s.base, cy);
         }
-        T P = f * k.t3 + s.f0 * k.t3 + s.f1 * (T(4) * k.t3) + s.base;
-        s.base = P;
+        const T inc = f * k.t3 + s.f0 * k.t3 + s.f1 * (T(4) * k.t3);
+        acc_add(s.base, s.blo, inc);
         s.f0 = f;
-        return add_carry(P, cy);
+        return add_carry(s.base + s.blo, cy);
     } else if (RULE == R_TRAP) {
-        T P = f * k.h + s.f0 * k.h + s.base;
-        s.base = P;
+        acc_add(s.base, s.blo, f * k.h + s.f0 * k.h);
         s.f0 = f;
-        return add_carry(P, cy);
+        return add_carry(s.base + s.blo, cy);
     } else {
-        T P = f * k.dt + s.base;
-        s.base = P;
-        return add_carry(P, cy);
+        acc_add(s.base, s.blo, f * k.dt);
+        return add_carry(s.base + s.blo, cy);
     }
 }
 
 // Adjoint of the block rules, processing positions from the chunk end
-// downwards.  Rb: LOCAL cotangent on the current anchor prefix from later
-// samples of the chunk (the cotangent rho from beyond the chunk is the carry
-// cy, added where totals are used); pend: cotangent on the anchor's f from
-// its use as the first sample of the later block.  Input H: local cotangent
-// on P[li]; returns the cotangent on f[li].
+// downwards.  Rb (+ rlo): LOCAL cotangent on the current anchor prefix from
+// later samples of the chunk (the cotangent rho from beyond the chunk is the
+// carry cy, added where totals are used); pend: cotangent on the anchor's f
+// from its use as the first sample of the later block.  Input H: local
+// cotangent on P[li]; returns the cotangent on f[li].
 template <class T>
 struct RevState {
-    T Rb, pend, R4l, R4, H2, H3;
+    T Rb, rlo, pend, R4l, R4, H2, H3;
 };
 
 template <class T, int RULE>
@@ -272,40 +304,38 @@ __device__ __forceinline__ T rev_step(RevState<T>& s, T H, int li, const RuleCoe
     if (RULE == R_BOOLE) {
         switch (li & 3) {
             case 0: {
-                s.R4l = H + s.Rb;
-                s.R4 = add_carry(s.R4l, cy);
+                s.R4l = H;  // block-local part; the anchor total is Rb + rlo + H
+                s.R4 = add_carry((H + s.rlo) + s.Rb, cy);
                 return s.R4 * k.b14 + s.pend;
             }
             case 3: s.H3 = H; return H * k.c38 + s.R4 * k.b64;
             case 2: s.H2 = H; return H * k.t3 + s.H3 * k.c98 + s.R4 * k.b24;
             default: {
-                T G = H * k.h + s.H2 * k.c4_3 + s.H3 * k.c98 + s.R4 * k.b64;
+                const T G = H * k.h + s.H2 * k.c4_3 + s.H3 * k.c98 + s.R4 * k.b64;
                 s.pend = H * k.h + s.H2 * k.t3 + s.H3 * k.c38 + s.R4 * k.b14;
-                s.Rb = H + s.H2 + s.H3 + s.R4l;
+                acc_add(s.Rb, s.rlo, H + s.H2 + s.H3 + s.R4l);
                 return G;
             }
         }
     } else if (RULE == R_SIMPSON) {
         if ((li & 1) == 0) {
-            s.R4l = H + s.Rb;
-            s.R4 = add_carry(s.R4l, cy);
+            s.R4l = H;
+            s.R4 = add_carry((H + s.rlo) + s.Rb, cy);
             return s.R4 * k.t3 + s.pend;
         }
-        T G = H * k.h + s.R4 * (T(4) * k.t3);
+        const T G = H * k.h + s.R4 * (T(4) * k.t3);
         s.pend = H * k.h + s.R4 * k.t3;
-        s.Rb = H + s.R4l;
+        acc_add(s.Rb, s.rlo, H + s.R4l);
         return G;
     } else if (RULE == R_TRAP) {
-        T Rl = H + s.Rb;
-        T Rt = add_carry(Rl, cy);
-        T G = Rt * k.h + s.pend;
-        s.Rb = Rl;
+        acc_add(s.Rb, s.rlo, H);
+        const T Rt = add_carry(s.Rb + s.rlo, cy);
+        const T G = Rt * k.h + s.pend;
         s.pend = Rt * k.h;
         return G;
     } else {
-        T Rl = H + s.Rb;
-        s.Rb = Rl;
-        return add_carry(Rl, cy) * k.dt;
+        acc_add(s.Rb, s.rlo, H);
+        return add_carry(s.Rb + s.rlo, cy) * k.dt;
     }
 }
 

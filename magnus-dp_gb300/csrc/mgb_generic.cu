@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
         const int first = riem0 ? 0 : 1;
         const int64_t Lm = (int64_t)L * m;
         const int64_t nm = (int64_t)n * m;
-        const RuleCoef<T> kc(I.dt);
+        const RuleCoef<T> kc(I.dt_k);
 
         T* Ab = slot;             // [L][m]   A over the chunk
         T* tape = Ab + Lm;        // [n-1][L][m]  P_j over the chunk
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
                 const double pij = (MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el];
                 const Carry<T> cy = split_carry<T>(pij);
                 FwdState<T> s;
-                s.base = T(0);
+                s.base = s.blo = T(0);
                 s.f0 = F[el];
                 s.f1 = s.f2 = s.f3 = T(0);
                 if (!riem0 && keep) Pj[el] = add_carry(T(0), cy);
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
                     const T P = fwd_step<T, RULE>(s, F[(int64_t)li * m + el], li, kc, cy);
                     if (keep) Pj[(int64_t)li * m + el] = P;
                 }
-                if (MODE == MODE_LOCAL) I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] = (double)s.base;
+                if (MODE == MODE_LOCAL) I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] = (double)s.base + (double)s.blo;
             }
             __syncthreads();
             if (j < n) {
@@ -103,9 +103,11 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
                 const int k = 2 + (int)(t % (n - 1)); t /= (n - 1);
                 const int q = (int)t;
                 T acc = T(0);
+                double sj = 1.0;
                 for (int j = 1; j <= k - 1; ++j) {
+                    sj *= I.sig;
                     const double* Dq = I.dq + ((int64_t)q * n + (k - j - 1)) * m;
-                    acc += A_::mul(tape + (int64_t)(j - 1) * Lm + (int64_t)li * m, Dq, d, el);
+                    acc += (T)sj * A_::mul(tape + (int64_t)(j - 1) * Lm + (int64_t)li * m, Dq, d, el);
                 }
                 if (KIND == KIND_SC && (k & 1)) acc = -acc;
                 const int64_t off = (((int64_t)q * (n - 1) + (k - 2)) * S + (b + li)) * m + el;
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
                 for (int el = threadIdx.x; el < m; el += NT) {
                     const Carry<T> cy = split_carry<T>(rc[(int64_t)(j - 1) * m + el]);
                     RevState<T> s;
-                    s.Rb = s.pend = s.R4l = s.R4 = s.H2 = s.H3 = T(0);
+                    s.Rb = s.rlo = s.pend = s.R4l = s.R4 = s.H2 = s.H3 = T(0);
                     for (int li = Kp; li >= first; --li) {
                         const T H = (j < n) ? Hb[(int64_t)li * m + el] : T(0);
                         Gb[(int64_t)li * m + el] = rev_step<T, RULE>(s, H, li, kc, cy);
@@ -194,7 +196,15 @@ __global__ void __launch_bounds__(NT) k_fin_fwd(const InstDev* __restrict__ inst
     const InstDev& I = insts[blockIdx.x];
     const int m = I.m, d = I.d, n = I.n, Q = I.Q;
     const int64_t nm = (int64_t)n * m;
-    const double* T_ = I.pi + (int64_t)I.C * nm;
+    {
+        const double* Tk = I.pi + (int64_t)I.C * nm;
+        for (int64_t idx = threadIdx.x; idx < nm; idx += NT) {
+            const int j = 1 + (int)(idx / m);
+            I.tt[idx] = Tk[idx] * pow(I.sig, (double)j);
+        }
+        __syncthreads();
+    }
+    const double* T_ = I.tt;
     for (int q = 0; q < Q; ++q) {
         double* Dq = I.dq + (int64_t)q * nm;
         const double s = I.glx[q] - 1.0;
@@ -262,7 +272,7 @@ __global__ void __launch_bounds__(NT) k_fin_vjp(const InstDev* __restrict__ inst
     const int m = I.m, d = I.d, n = I.n, Q = I.Q;
     const int64_t nm = (int64_t)n * m;
     const bool f64 = f64io != 0;
-    const double* T_ = I.pi + (int64_t)I.C * nm;
+    const double* T_ = I.tt;
     // Omega-bar (SpaceCurve: padded, signed)
     for (int64_t idx = threadIdx.x; idx < nm; idx += NT) {
         const int k = 1 + (int)(idx / m), el = (int)(idx % m);
@@ -319,6 +329,11 @@ __global__ void __launch_bounds__(NT) k_fin_vjp(const InstDev* __restrict__ inst
             }
             __syncthreads();
         }
+    }
+    // cotangent on the kernels' unscaled totals: d/dT~_j = sig^j d/dT_j
+    for (int64_t idx = threadIdx.x; idx < nm; idx += NT) {
+        const int j = 1 + (int)(idx / m);
+        I.tau[idx] *= pow(I.sig, (double)j);
     }
 }
 

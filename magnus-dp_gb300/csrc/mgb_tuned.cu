@@ -107,8 +107,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
     float* const sPT = sA + G * D * P4;  // reverse: P^T   [G][D][P4]
     float* const sG = sPT + G * D * P4;  // reverse: G     [G][D][P1]
     float* const sH = sG + G * D * P1;   // reverse: H     [G][D][P1]
-    float* const st = sm + Cf::OPND;     // state [n][2][m]
-    float* const tape = scratch + (int64_t)blockIdx.x * slot_elems;
+    float* const slot = scratch + (int64_t)blockIdx.x * slot_elems;
 
     const int tid = threadIdx.x;
     const int tl = tid / TPS, tu = tid % TPS;
@@ -124,17 +123,21 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
         const bool riem0 = (RULE == R_RIEMANN) && c == 0;
         const int first = riem0 ? 0 : 1;
         const int64_t nm = (int64_t)n * m;
-        const RuleCoef<float> kc(I.dt);
+        const RuleCoef<float> kc(I.dt_k);
         const double* pic = I.pi + (int64_t)c * nm;
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         const int NLf = (MODE == MODE_LOCAL) ? n : n - 1;  // levels with a forward prefix
+        // per-level prefix state [n][3][m] (L2-resident), then the tape [n-1][L][m]
+        float* const st = slot;
+        float* const tape = slot + (int64_t)3 * n * m;
 
         // ---------------- forward state at the chunk start ----------------
         for (int j = 1; j <= NLf; ++j)
             for (int q = 0; q < EPT; ++q) {
                 const int el = tid + q * TNT;
-                st[(j - 1) * 2 * m + el] = 0.f;
-                st[(j - 1) * 2 * m + m + el] = (j == 1) ? __ldg(Ag + el) : 0.f;
+                st[(j - 1) * 3 * m + el] = 0.f;
+                st[(j - 1) * 3 * m + m + el] = 0.f;
+                st[(j - 1) * 3 * m + 2 * m + el] = (j == 1) ? __ldg(Ag + el) : 0.f;
             }
         if (MODE == MODE_VJP && !riem0 && NLf >= 2) {
             // f0_j = A[b] P_{j-1}[b] = A[b] pi_{j-1} for j = 2..NLf
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                 if (j0 + tl <= NLf) {
                     float acc[4][4] = {};
                     mma_tv<D>(acc, sAT, P4, sP + tl * D * P4, P4, r0, c0);
-                    float* f0 = st + (j0 + tl - 1) * 2 * m + m;
+                    float* f0 = st + (j0 + tl - 1) * 3 * m + 2 * m;
 #pragma unroll
                     for (int t = 0; t < 4; ++t)
 #pragma unroll
@@ -182,10 +185,11 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                     const int el = tid + q * TNT, r = el / D, cc = el % D;
                     const Carry<float> cy =
                         split_carry<float>((MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el]);
-                    float* sj = st + (j - 1) * 2 * m;
+                    float* sj = st + (j - 1) * 3 * m;
                     FwdState<float> s;
                     s.base = sj[el];
-                    s.f0 = sj[m + el];
+                    s.blo = sj[m + el];
+                    s.f0 = sj[2 * m + el];
                     s.f1 = s.f2 = s.f3 = 0.f;
                     for (int l = 0; l < ge; ++l) {
                         const float P = fwd_step<float, RULE>(s, sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
@@ -193,7 +197,8 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                         if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
                     }
                     sj[el] = s.base;
-                    sj[m + el] = s.f0;
+                    sj[m + el] = s.blo;
+                    sj[2 * m + el] = s.f0;
                 }
                 __syncthreads();
                 if (j < NLf) {
@@ -214,7 +219,8 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             for (int j = 1; j <= n; ++j)
                 for (int q = 0; q < EPT; ++q) {
                     const int el = tid + q * TNT;
-                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] = (double)st[(j - 1) * 2 * m + el];
+                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] =
+                        (double)st[(j - 1) * 3 * m + el] + (double)st[(j - 1) * 3 * m + m + el];
                 }
         }
 
@@ -224,8 +230,9 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             for (int j = 1; j <= n; ++j)
                 for (int q = 0; q < EPT; ++q) {
                     const int el = tid + q * TNT;
-                    st[(j - 1) * 2 * m + el] = 0.f;      // Rb (local)
-                    st[(j - 1) * 2 * m + m + el] = 0.f;  // pend
+                    st[(j - 1) * 3 * m + el] = 0.f;          // Rb (local)
+                    st[(j - 1) * 3 * m + m + el] = 0.f;      // its compensation
+                    st[(j - 1) * 3 * m + 2 * m + el] = 0.f;  // pend
                 }
             float* dAg = static_cast<float*>(I.dA) + b * m;
             const int last0 = first + ((Kp - first) / G) * G;
@@ -263,17 +270,19 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                     for (int q = 0; q < EPT; ++q) {
                         const int el = tid + q * TNT, r = el / D, cc = el % D;
                         const Carry<float> cy = split_carry<float>(rc[(int64_t)(j - 1) * m + el]);
-                        float* sj = st + (j - 1) * 2 * m;
+                        float* sj = st + (j - 1) * 3 * m;
                         RevState<float> s;
                         s.Rb = sj[el];
-                        s.pend = sj[m + el];
+                        s.rlo = sj[m + el];
+                        s.pend = sj[2 * m + el];
                         s.R4l = s.R4 = s.H2 = s.H3 = 0.f;
                         for (int l = ge - 1; l >= 0; --l) {
                             const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
                             sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(s, H, li0 + l, kc, cy);
                         }
                         sj[el] = s.Rb;
-                        sj[m + el] = s.pend;
+                        sj[m + el] = s.rlo;
+                        sj[2 * m + el] = s.pend;
                     }
                     __syncthreads();
                 }
@@ -304,7 +313,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                 for (int j = 1; j < n; ++j) {
                     for (int el = tid; el < m; el += TNT) {
                         const int r = el / D, cc = el % D;
-                        sG[r * P1 + cc] = st[j * 2 * m + m + el];
+                        sG[r * P1 + cc] = st[j * 3 * m + 2 * m + el];
                         sPT[cc * P4 + r] = (float)pic[(int64_t)(j - 1) * m + el];
                     }
                     __syncthreads();
@@ -318,7 +327,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             const int el = (r0 + t) * D + c0 + u;
-                            const float v = bacc[t][u] + st[m + el];
+                            const float v = bacc[t][u] + st[2 * m + el];
                             if (c > 0) atomicAdd(row + el, v);
                             else row[el] = v;
                         }
@@ -330,8 +339,8 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
 }
 
 template <int D>
-size_t tile_smem_bytes(int nmax) {
-    return ((size_t)TileCfg<D>::OPND + 2 * (size_t)nmax * TileCfg<D>::m) * sizeof(float);
+size_t tile_smem_bytes(int) {
+    return (size_t)TileCfg<D>::OPND * sizeof(float);
 }
 
 template <int D, int RULE, int MODE>

@@ -123,8 +123,13 @@ def test_mixed_spacecurve_within_1e6(cuda):
                                      dtype=np.float64)[0]
     ref = O.forward_sc(F, 6, 0.0, 2.0, "many", "Simpson")
     out = core.compute_sc(6, F, 0.0, 2.0, op="many", integrator="Simpson", precision="mixed")
+    scale = max(np.linalg.norm(r) for r in ref)
     for k in range(6):
-        assert rel(out[k], ref[k]) <= 1e-6, (k, rel(out[k], ref[k]))
+        # Omega_1 of whole-period sinusoids is zero analytically (~1e-15 here):
+        # orders that vanish are measured against the largest order instead.
+        den = max(np.linalg.norm(ref[k]), 1e-6 * scale)
+        err = np.linalg.norm(out[k] - ref[k]) / den
+        assert err <= 1e-6, (k, err)
 
 
 @pytest.mark.parametrize("op", ["one", "many", "sum"])
