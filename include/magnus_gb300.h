@@ -103,6 +103,25 @@ mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* c
 mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void* carry);
 mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, void* dA);
 
+/* Forward that allocates no device memory.  For callers that cannot call
+ * cudaMalloc during their work — an XLA/JAX custom call, or any framework
+ * whose caching allocator already holds the GPU's memory, or a host that must
+ * not allocate (or synchronize the device) mid-run.  Same result as
+ * mgb_forward(p, A, out, NULL, NULL, stream) (no carry, no checkpoints), but
+ * every piece of working memory comes from one array of
+ * MGB_NOALLOC_SCRATCH_BYTES compiled into the library, which each GPU that
+ * loads the library holds until the process exits.  A problem whose
+ * workspace does not fit is rejected with MGB_ERR_INVALID_ARGUMENT and a
+ * message giving the bytes it needs.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress with that device current); make
+ * that first call before any stream capture.  All calls on a device share the
+ * array and it keeps the previous call's contents (nothing needs clearing);
+ * calls whose GPU work can overlap race on it, so order them on one stream.
+ * No counterpart in the reference (its CPU code allocates on the host heap).
+ * A and out are device pointers; the call is stream-ordered. */
+#define MGB_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, void* out, void* stream);
+
 /* Gauss-Legendre table: weights/nodes on [0, 1] for orders 1..max_order,
  * order q at offset q(q-1)/2 (flattened like the reference).  Copied. */
 mgb_status mgb_set_gl_table(size_t max_order, const double* weights, const double* nodes);

@@ -609,3 +609,155 @@ size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset) {
 int mgb_version(void) { return 1; }
 
 }  // extern "C"
+
+// ============================================================================
+// Forward that allocates no device memory: mgb_forward_noalloc.
+//
+// Some callers cannot call cudaMalloc in the middle of their work: an XLA /
+// JAX custom call or another framework whose caching allocator already owns
+// (nearly) all of the GPU's memory, or a host that forbids device-memory
+// allocation while it is running (a real-time loop, a callback that must not
+// synchronize the device).  For them this entry point keeps all of its
+// working memory — the call's descriptors, chunk work list, Gauss-Legendre
+// values, chunk checkpoints, per-instance small-math buffers and the chunk
+// kernels' per-CTA slots — in one fixed array compiled into this library,
+// g_noalloc_scratch below.  The array's size is fixed (MGB_NOALLOC_SCRATCH_BYTES,
+// 64 MiB), so every GPU that loads the library holds it until the process
+// exits, and problems whose workspace does not fit are rejected.
+//
+// Sharing: every call on a device uses the same array and leaves its contents
+// behind for the next call.  No part of it has to start at zero (each kernel
+// writes what it reads first), so nothing is cleared between calls.  Calls
+// whose GPU work can overlap (different streams without ordering between
+// them) race on the array; order them on one stream or synchronize between
+// them.
+// ============================================================================
+namespace {
+
+constexpr size_t kNoAllocBytes = (size_t)64 << 20;
+static_assert(kNoAllocBytes == MGB_NOALLOC_SCRATCH_BYTES, "keep the header constant in sync");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+__global__ void k_noalloc_work(ChunkRef* work, int C) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) work[c] = ChunkRef{0, c};
+}
+
+std::mutex g_noalloc_mutex;
+std::vector<void*> g_noalloc_base;  // device address of g_noalloc_scratch, per device ordinal
+
+// Device address of the array on the current device.  The first call on a
+// device looks it up with cudaGetSymbolAddress (with that device current);
+// later calls reuse the cached address.
+mgb_status noalloc_base(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(MGB_ERR_CUDA, std::string(cudaGetErrorString(e)) + " in cudaGetDevice");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if ((int)g_noalloc_base.size() <= dev) g_noalloc_base.resize(dev + 1, nullptr);
+    if (!g_noalloc_base[dev]) {
+        void* ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(MGB_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
+        g_noalloc_base[dev] = ptr;
+    }
+    *out = g_noalloc_base[dev];
+    return MGB_OK;
+}
+
+}  // namespace
+
+extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, void* out, void* stream) {
+    g_last_error.clear();
+    auto gl = gl_snapshot();
+    Derived v;
+    mgb_status st = validate(p, gl->max_order, &v);
+    if (st != MGB_OK) return st;
+    if (!A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+    if (!out) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    const bool plain = p->precision == MGB_PRECISION_PLAIN;
+    const int f64io = p->dtype == MGB_DTYPE_F64;
+    const size_t tsz = plain ? sizeof(double) : sizeof(float);
+
+    // layout inside the fixed array (same pieces as a regular call)
+    const int64_t L = std::min<int64_t>((int64_t)v.K, (int64_t)p->samples - 1) + 1;
+    const int64_t slot_elems = (int64_t)(p->n + 4) * L * v.m + 3 * (int64_t)p->n * v.m;
+    size_t off = 0;
+    const size_t off_inst = off; off = align_up(off + sizeof(InstDev), 256);
+    const size_t off_work = off; off = align_up(off + (size_t)v.C * sizeof(ChunkRef), 256);
+    const size_t off_gl = off; off = align_up(off + 2 * (size_t)v.Q * sizeof(double), 256);
+    const size_t off_ck = off; off = align_up(off + ckpt_doubles(*p, v) * sizeof(double), 256);
+    const size_t off_ws = off; off = align_up(off + ws_doubles(v) * sizeof(double), 256);
+    const size_t off_scr = off;
+    const size_t slot_bytes = (size_t)slot_elems * tsz;
+    if (off_scr + slot_bytes > kNoAllocBytes)
+        return fail(MGB_ERR_INVALID_ARGUMENT,
+                    "problem needs " + std::to_string(off_scr + slot_bytes) +
+                        " bytes of workspace; mgb_forward_noalloc is limited to MGB_NOALLOC_SCRATCH_BYTES (" +
+                        std::to_string(kNoAllocBytes) + ")");
+    const DevInfo di = device_info();
+    int64_t grid = std::min<int64_t>((int64_t)v.C, (int64_t)di.sms * 8);
+    grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)((kNoAllocBytes - off_scr) / slot_bytes)));
+
+    void* basev = nullptr;
+    st = noalloc_base(&basev);
+    if (st != MGB_OK) return st;
+    char* base = static_cast<char*>(basev);
+
+    InstDev I;
+    std::memset(&I, 0, sizeof(I));
+    double* ck = reinterpret_cast<double*>(base + off_ck);
+    double* w = reinterpret_cast<double*>(base + off_ws);
+    I.A = A;
+    I.out = out;
+    I.pi = ck;
+    I.lam = ck + (size_t)(v.C + 1) * v.nm;
+    I.rho = w; w += (size_t)v.C * v.nm;
+    I.dq = w; w += (size_t)v.Q * v.nm;
+    I.ee = w; w += v.nm;
+    I.tau = w; w += v.nm;
+    I.ob = w; w += v.nm;
+    I.eb = w; w += v.nm;
+    I.db = w; w += v.nm;
+    I.tt = w; w += v.nm;
+    double* g = reinterpret_cast<double*>(base + off_gl);
+    I.glw = g;
+    I.glx = g + v.Q;
+    I.dt = (p->tf - p->t0) / (double)(p->samples - 1);
+    I.dt_k = kernel_step(*p, I.dt);
+    I.sig = (I.dt_k != 0.0) ? I.dt / I.dt_k : 1.0;
+    I.S = (int64_t)p->samples;
+    I.d = (p->kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p->dim;
+    I.m = v.m;
+    I.n = (int32_t)p->n;
+    I.C = v.C;
+    I.Q = v.Q;
+    I.K = v.K;
+    I.op = p->op;
+    const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
+    // pageable sources: each copy is staged before cudaMemcpyAsync returns
+    MGB_CUDA_TRY(cudaMemcpyAsync(base + off_inst, &I, sizeof(InstDev), cudaMemcpyHostToDevice, cs));
+    MGB_CUDA_TRY(cudaMemcpyAsync(g, gl->w.data() + go, (size_t)v.Q * sizeof(double), cudaMemcpyHostToDevice, cs));
+    MGB_CUDA_TRY(cudaMemcpyAsync(g + v.Q, gl->x.data() + go, (size_t)v.Q * sizeof(double), cudaMemcpyHostToDevice, cs));
+    ChunkRef* d_work = reinterpret_cast<ChunkRef*>(base + off_work);
+    k_noalloc_work<<<(unsigned)std::min<int64_t>((v.C + 255) / 256, 1024), 256, 0, cs>>>(d_work, v.C);
+    MGB_CUDA_TRY(cudaGetLastError());
+
+    const InstDev* d_inst = reinterpret_cast<const InstDev*>(base + off_inst);
+    LaunchArgs la;
+    la.insts = d_inst;
+    la.work = d_work;
+    la.nwork = v.C;
+    la.scratch = base + off_scr;
+    la.slot_elems = slot_elems;
+    la.grid = grid;
+    la.f64io = f64io;
+    la.stream = cs;
+    const std::vector<InstDev> hi(1, I);
+    MGB_CUDA_TRY(launch_chunk_any(plain, p->kind, p->integrator, MODE_LOCAL, la, hi, di.sms));
+    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_SCAN, d_inst, 1, f64io, 0, cs));
+    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_FIN_FWD, d_inst, 1, f64io, 1, cs));
+    return MGB_OK;
+}

@@ -63,6 +63,7 @@ SIGNATURES = {
     "mgb_max_order": (ctypes.c_size_t, []),
     "mgb_last_error": (ctypes.c_char_p, []),
     "mgb_version": (ctypes.c_int, []),
+    "mgb_forward_noalloc": (ctypes.c_int, [_PP, _VP, _VP, _VP]),
     "mgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "mgb_profile_read": (ctypes.c_size_t, [ctypes.POINTER(KernelTime), ctypes.c_size_t, ctypes.c_int]),
 }
