@@ -70,14 +70,18 @@ def load_peaks():
     return 6800.0, 1900.0, 2070.0, "fallback"
 
 
-def traffic_from_profiles(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+def traffic_from_profiles(kernel, scale=1.0):
+    """Per-launch DRAM bytes of `kernel` (full config4 launch) from the committed
+    ncu summary profiles/traffic.txt, scaled to the launch being measured."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        t = json.load(f)
-    return t.get(kernel)
+        for line in f:
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#") and parts[0] == kernel:
+                return float(parts[1]) * scale
+    return None
 
 
 class ClockSampler:
@@ -272,7 +276,8 @@ def main():
         roof = {"bound": "tensor", "achieved": tflops, "peak": bf16_peak, "unit": "TFLOP/s", "frac": tflops / bf16_peak}
     else:
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak}
-    roof.update({"kernel": dom_name, "traffic": traffic_from_profiles(dom_name), "peak_source": peak_src,
+    units_scale = (B * S) / (CONFIG4["batch"] * CONFIG4["samples"])
+    roof.update({"kernel": dom_name, "traffic": traffic_from_profiles(dom_name, units_scale), "peak_source": peak_src,
                  "launch_ms": dom_ms, "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": bytes_alg,
                  "fp32_simt": {"achieved_tflops": tflops, "nominal_peak_tflops": fp32_peak,
                                "frac": tflops / fp32_peak}})
