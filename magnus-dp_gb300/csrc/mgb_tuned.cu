@@ -166,39 +166,55 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
         for (int li0 = first; li0 <= Kp; li0 += G) {
             const int ge = min(G, Kp - li0 + 1);
             {
+                constexpr int NV = G * m / 4 / TNT;  // float4 per thread
                 const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
-                for (int i4 = tid; i4 < ge * m / 4; i4 += TNT) {
-                    const float4 v = __ldg(src + i4);
+                float4 v[NV];
+#pragma unroll
+                for (int q = 0; q < NV; ++q) {
+                    const int i4 = tid + q * TNT;
+                    v[q] = (i4 * 4 < ge * m) ? __ldg(src + i4) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int q = 0; q < NV; ++q) {
+                    const int i4 = tid + q * TNT;
                     const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                    *reinterpret_cast<float4*>(sF + l * D * P4 + r * P4 + cc) = v;
+                    *reinterpret_cast<float4*>(sF + l * D * P4 + r * P4 + cc) = v[q];
                     float* at = sAT + l * D * P4 + r;
-                    at[(cc + 0) * P4] = v.x;
-                    at[(cc + 1) * P4] = v.y;
-                    at[(cc + 2) * P4] = v.z;
-                    at[(cc + 3) * P4] = v.w;
+                    at[(cc + 0) * P4] = v[q].x;
+                    at[(cc + 1) * P4] = v[q].y;
+                    at[(cc + 2) * P4] = v[q].z;
+                    at[(cc + 3) * P4] = v[q].w;
                 }
             }
             __syncthreads();
             for (int j = 1; j <= NLf; ++j) {
-#pragma unroll
-                for (int q = 0; q < EPT; ++q) {
-                    const int el = tid + q * TNT, r = el / D, cc = el % D;
-                    const Carry<float> cy =
-                        split_carry<float>((MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el]);
+                {
                     float* sj = st + (j - 1) * 3 * m;
-                    FwdState<float> s;
-                    s.base = sj[el];
-                    s.blo = sj[m + el];
-                    s.f0 = sj[2 * m + el];
-                    s.f1 = s.f2 = s.f3 = 0.f;
-                    for (int l = 0; l < ge; ++l) {
-                        const float P = fwd_step<float, RULE>(s, sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
-                        sP[l * D * P4 + r * P4 + cc] = P;
-                        if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
+                    FwdState<float> s[EPT];
+                    double pv[EPT];
+#pragma unroll
+                    for (int q = 0; q < EPT; ++q) {  // all global loads first
+                        const int el = tid + q * TNT;
+                        s[q].base = sj[el];
+                        s[q].blo = sj[m + el];
+                        s[q].f0 = sj[2 * m + el];
+                        s[q].f1 = s[q].f2 = s[q].f3 = 0.f;
+                        pv[q] = (MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el];
                     }
-                    sj[el] = s.base;
-                    sj[m + el] = s.blo;
-                    sj[2 * m + el] = s.f0;
+#pragma unroll
+                    for (int q = 0; q < EPT; ++q) {
+                        const int el = tid + q * TNT, r = el / D, cc = el % D;
+                        const Carry<float> cy = split_carry<float>(pv[q]);
+                        for (int l = 0; l < ge; ++l) {
+                            const float P = fwd_step<float, RULE>(s[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
+                            sP[l * D * P4 + r * P4 + cc] = P;
+                            // tape rows hold P^T so the adjoint reloads them contiguously
+                            if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + cc * D + r] = P;
+                        }
+                        sj[el] = s[q].base;
+                        sj[m + el] = s[q].blo;
+                        sj[2 * m + el] = s[q].f0;
+                    }
                 }
                 __syncthreads();
                 if (j < NLf) {
@@ -239,20 +255,37 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             for (int li0 = last0; li0 >= first; li0 -= G) {
                 const int ge = min(G, Kp - li0 + 1);
                 {
+                    constexpr int NV = G * m / 4 / TNT;
                     const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
-                    for (int i4 = tid; i4 < ge * m / 4; i4 += TNT) {
-                        const float4 v = __ldg(src + i4);
+                    float4 v[NV];
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) {
+                        const int i4 = tid + q * TNT;
+                        v[q] = (i4 * 4 < ge * m) ? __ldg(src + i4) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int q = 0; q < NV; ++q) {
+                        const int i4 = tid + q * TNT;
                         const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                        *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = v;
+                        *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = v[q];
                     }
                 }
                 float dacc[4][4] = {};
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
-                        const float* src = tape + ((int64_t)(j - 1) * L + li0) * m;
-                        for (int idx = tid; idx < ge * m; idx += TNT) {
-                            const int l = idx / m, el = idx % m, r = el / D, cc = el % D;
-                            sPT[l * D * P4 + cc * P4 + r] = src[idx];
+                        constexpr int NV = G * m / 4 / TNT;
+                        const float4* src = reinterpret_cast<const float4*>(tape + ((int64_t)(j - 1) * L + li0) * m);
+                        float4 v[NV];
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) {
+                            const int i4 = tid + q * TNT;
+                            v[q] = (i4 * 4 < ge * m) ? src[i4] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) {
+                            const int i4 = tid + q * TNT;
+                            const int l = (i4 * 4) / m, el = (i4 * 4) % m, k = el / D, cc = el % D;
+                            *reinterpret_cast<float4*>(sPT + l * D * P4 + k * P4 + cc) = v[q];
                         }
                         __syncthreads();
                         if (tl < ge) {
@@ -266,23 +299,31 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                         }
                     }
                     __syncthreads();
-#pragma unroll
-                    for (int q = 0; q < EPT; ++q) {
-                        const int el = tid + q * TNT, r = el / D, cc = el % D;
-                        const Carry<float> cy = split_carry<float>(rc[(int64_t)(j - 1) * m + el]);
+                    {
                         float* sj = st + (j - 1) * 3 * m;
-                        RevState<float> s;
-                        s.Rb = sj[el];
-                        s.rlo = sj[m + el];
-                        s.pend = sj[2 * m + el];
-                        s.R4l = s.R4 = s.H2 = s.H3 = 0.f;
-                        for (int l = ge - 1; l >= 0; --l) {
-                            const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
-                            sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(s, H, li0 + l, kc, cy);
+                        RevState<float> s[EPT];
+                        double rv[EPT];
+#pragma unroll
+                        for (int q = 0; q < EPT; ++q) {  // all global loads first
+                            const int el = tid + q * TNT;
+                            s[q].Rb = sj[el];
+                            s[q].rlo = sj[m + el];
+                            s[q].pend = sj[2 * m + el];
+                            s[q].R4l = s[q].R4 = s[q].H2 = s[q].H3 = 0.f;
+                            rv[q] = rc[(int64_t)(j - 1) * m + el];
                         }
-                        sj[el] = s.Rb;
-                        sj[m + el] = s.rlo;
-                        sj[2 * m + el] = s.pend;
+#pragma unroll
+                        for (int q = 0; q < EPT; ++q) {
+                            const int el = tid + q * TNT, r = el / D, cc = el % D;
+                            const Carry<float> cy = split_carry<float>(rv[q]);
+                            for (int l = ge - 1; l >= 0; --l) {
+                                const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
+                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(s[q], H, li0 + l, kc, cy);
+                            }
+                            sj[el] = s[q].Rb;
+                            sj[m + el] = s[q].rlo;
+                            sj[2 * m + el] = s[q].pend;
+                        }
                     }
                     __syncthreads();
                 }

@@ -127,7 +127,7 @@ def test_mixed_spacecurve_within_1e6(cuda):
     for k in range(6):
         # Omega_1 of whole-period sinusoids is zero analytically (~1e-15 here):
         # orders that vanish are measured against the largest order instead.
-        den = max(np.linalg.norm(ref[k]), 1e-6 * scale)
+        den = np.linalg.norm(ref[k]) if np.linalg.norm(ref[k]) >= 1e-6 * scale else scale
         err = np.linalg.norm(out[k] - ref[k]) / den
         assert err <= 1e-6, (k, err)
 
