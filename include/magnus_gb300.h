@@ -99,6 +99,25 @@ mgb_status mgb_forward_batched(const mgb_problem* probs, size_t count, const voi
 mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* const* A, const void* const* cot,
                            const void* const* ckpt, void* const* dA, void* stream);
 
+/* Plans.  mgb_plan_create validates `count` problems, binds their device
+ * buffers (A; out for the forward; cot and dA for the VJP — either pair may
+ * be NULL) and prepares everything the engine needs on the device (one
+ * cudaMalloc, descriptors uploaded, instances of equal dimension grouped into
+ * segments that run concurrently).  mgb_plan_forward / mgb_plan_vjp then only
+ * enqueue kernels on `stream`, so they can be captured into a CUDA graph and
+ * replayed.  The VJP reuses the checkpoints of the plan's last forward (or
+ * recomputes them when the plan has not run forward yet).  Replaces the
+ * reference's KernelPlan { divisibility_requirement(); run(alloc) } made by
+ * make_plan / make_vjp_plan (src/composer/dispatch.hpp:446-492,
+ * src/composer/backends.cpp:65-102). */
+typedef struct mgb_plan mgb_plan;
+mgb_status mgb_plan_create(const mgb_problem* probs, size_t count, const void* const* A, void* const* out,
+                           const void* const* cot, void* const* dA, mgb_plan** plan);
+mgb_status mgb_plan_forward(mgb_plan* plan, void* stream);
+mgb_status mgb_plan_vjp(mgb_plan* plan, void* stream);
+size_t mgb_plan_bytes(const mgb_plan* plan);
+mgb_status mgb_plan_destroy(mgb_plan* plan);
+
 /* Host-pointer forms (synchronous; device staging inside). carry nullable. */
 mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void* carry);
 mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, void* dA);

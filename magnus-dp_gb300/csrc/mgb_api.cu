@@ -217,98 +217,196 @@ struct Call {
     cudaStream_t stream;
 };
 
-mgb_status run(const Call& call) {
-    if (call.count == 0) return MGB_OK;
+// ---------------------------------------------------------------- plans
+// A plan holds everything a call needs on the device: per-instance
+// descriptors, chunk work lists, Gauss-Legendre values, checkpoints, small
+// algebra workspace and per-CTA scratch, in one buffer.  Instances are sorted
+// by matrix dimension and cut into segments; each segment runs the fastest
+// chunk kernel that covers its shape (mgb_tuned.cu) or the generic kernel,
+// on its own stream when there are several segments.  After the one-time
+// upload, launching a plan only enqueues kernels (so it can be captured into
+// a CUDA graph).  This is the engine's counterpart of the reference's
+// KernelPlan made by make_plan / make_vjp_plan
+// (src/composer/dispatch.hpp:446-492, src/composer/backends.cpp:65-102).
+struct Segment {
+    int32_t first = 0, count = 0;  // instance range (sorted order)
+    int64_t work_off = 0, nwork = 0;
+    TunedChoice tc;
+    int64_t slot_elems = 0, grid = 0;
+    size_t scr_off = 0;
+    std::vector<InstDev> hi;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+struct PlanCore {
+    int kind = 0, rule = 0, f64io = 0;
+    bool plain = true;
+    size_t count = 0;
+    bool has_out = false, has_vjp = false, any_carry = false, all_ck_in = false;
+    std::vector<InstDev> hi;       // sorted order
+    std::vector<int32_t> order;    // sorted position -> caller index
+    std::vector<ChunkRef> work;
+    std::vector<double> gl;
+    std::vector<Segment> segs;
+    size_t off_inst = 0, off_work = 0, off_gl = 0, off_ck = 0, off_ws = 0, off_gscr = 0, bytes = 0;
+    int64_t gslot_elems = 0, ggrid = 0;  // generic scratch (carry record)
+    char* base = nullptr;
+    bool async_alloc = false;
+    cudaStream_t alloc_stream = nullptr;
+    cudaEvent_t fork = nullptr;
+    int sms = 1;
+
+    void release_streams() {
+        for (Segment& sg : segs) {
+            if (sg.stream) cudaStreamDestroy(sg.stream);
+            if (sg.done) cudaEventDestroy(sg.done);
+            sg.stream = nullptr;
+            sg.done = nullptr;
+        }
+        if (fork) cudaEventDestroy(fork);
+        fork = nullptr;
+    }
+};
+
+// Validate, sort, cut segments and compute the layout (no device work).
+mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv) {
+    if (call.count == 0) return fail(MGB_ERR_INVALID_ARGUMENT, "no problems given");
     if (!call.probs || !call.A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
     auto gl = gl_snapshot();
-    std::vector<Derived> dv(call.count);
+    dv.resize(call.count);
+    const mgb_problem& p0 = call.probs[0];
     for (size_t i = 0; i < call.count; ++i) {
         mgb_status st = validate(&call.probs[i], gl->max_order, &dv[i]);
         if (st != MGB_OK) return st;
-        const mgb_problem& p0 = call.probs[0];
         const mgb_problem& p = call.probs[i];
         if (p.kind != p0.kind || p.dtype != p0.dtype || p.precision != p0.precision || p.integrator != p0.integrator)
             return fail(MGB_ERR_INVALID_ARGUMENT, "batched instances must share kind, dtype, precision and integrator");
         if (!call.A[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
-        if (!call.vjp && (!call.out || !call.out[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
-        if (call.vjp && (!call.cot || !call.cot[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent buffer must not be null");
-        if (call.vjp && (!call.dA || !call.dA[i])) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+        if (call.out && !call.out[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+        if (call.cot && !call.cot[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent buffer must not be null");
+        if (call.dA && !call.dA[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
     }
-    const mgb_problem& p0 = call.probs[0];
-    const int kind = p0.kind;
-    const bool plain = p0.precision == MGB_PRECISION_PLAIN;
-    const int f64io = p0.dtype == MGB_DTYPE_F64;
-    const size_t tsz = plain ? sizeof(double) : sizeof(float);
+    if (!call.out && !call.dA) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    if ((call.cot == nullptr) != (call.dA == nullptr))
+        return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent and dA buffers must be given together");
+    pc.kind = p0.kind;
+    pc.rule = p0.integrator;
+    pc.plain = p0.precision == MGB_PRECISION_PLAIN;
+    pc.f64io = p0.dtype == MGB_DTYPE_F64;
+    pc.count = call.count;
+    pc.has_out = call.out != nullptr;
+    pc.has_vjp = call.dA != nullptr;
+    pc.sms = device_info().sms;
+    const size_t tsz = pc.plain ? sizeof(double) : sizeof(float);
 
-    // ---- sizes
-    const size_t n_inst = call.count;
+    // sort by dimension (largest first: heavy segments start first)
+    pc.order.resize(call.count);
+    for (size_t i = 0; i < call.count; ++i) pc.order[i] = (int32_t)i;
+    std::stable_sort(pc.order.begin(), pc.order.end(), [&](int32_t a, int32_t b) { return dv[a].m > dv[b].m; });
+
     size_t nwork = 0, gl_doubles = 0, ck_doubles = 0, wsd = 0;
-    int64_t slot_elems = 0;
-    bool any_carry = false;
-    for (size_t i = 0; i < n_inst; ++i) {
-        const mgb_problem& p = call.probs[i];
+    pc.all_ck_in = call.ckpt_in != nullptr;
+    for (size_t i = 0; i < call.count; ++i) {
         nwork += (size_t)dv[i].C;
         gl_doubles += 2 * (size_t)dv[i].Q;
-        const bool user_ck = call.vjp ? (call.ckpt_in && call.ckpt_in[i]) : (call.ckpt_out && call.ckpt_out[i]);
-        if (!user_ck) ck_doubles += ckpt_doubles(p, dv[i]);
+        const bool user_ck = (call.ckpt_in && call.ckpt_in[i]) || (call.ckpt_out && call.ckpt_out[i]);
+        if (!user_ck) ck_doubles += ckpt_doubles(call.probs[i], dv[i]);
+        if (call.ckpt_in && !call.ckpt_in[i]) pc.all_ck_in = false;
         wsd += ws_doubles(dv[i]);
-        const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
-        slot_elems = std::max<int64_t>(slot_elems, (int64_t)(p.n + 4) * L * dv[i].m + 3 * (int64_t)p.n * dv[i].m);
-        if (!call.vjp && call.carry && call.carry[i]) any_carry = true;
+        if (call.carry && call.carry[i]) pc.any_carry = true;
     }
     if (nwork > (size_t)std::numeric_limits<int32_t>::max()) return fail(MGB_ERR_INVALID_ARGUMENT, "input shape is too large");
 
-    const DevInfo di = device_info();
+    // segments: runs of equal dimension
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 4, (size_t)16 << 30));
-    const size_t slot_bytes = (size_t)slot_elems * tsz;
-    int64_t grid = std::min<int64_t>((int64_t)nwork, (int64_t)di.sms * 8);
-    grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)(budget / std::max<size_t>(slot_bytes, 1))));
-
+    int64_t wpos = 0;
+    for (size_t a = 0; a < call.count;) {
+        size_t b = a;
+        while (b < call.count && dv[pc.order[b]].m == dv[pc.order[a]].m) ++b;
+        Segment sg;
+        sg.first = (int32_t)a;
+        sg.count = (int32_t)(b - a);
+        sg.work_off = wpos;
+        for (size_t k = a; k < b; ++k) {
+            const int32_t i = pc.order[k];
+            const mgb_problem& p = call.probs[i];
+            sg.nwork += dv[i].C;
+            const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
+            sg.slot_elems = std::max<int64_t>(sg.slot_elems, (int64_t)(p.n + 4) * L * dv[i].m + 3 * (int64_t)p.n * dv[i].m);
+        }
+        wpos += sg.nwork;
+        pc.segs.push_back(std::move(sg));
+        a = b;
+    }
+    // scratch budget shared by the segments in proportion to their work
     size_t off = 0;
-    const size_t off_inst = off; off = align_up(off + n_inst * sizeof(InstDev), 256);
-    const size_t off_work = off; off = align_up(off + nwork * sizeof(ChunkRef), 256);
-    const size_t off_gl = off; off = align_up(off + gl_doubles * sizeof(double), 256);
-    const size_t off_ck = off; off = align_up(off + ck_doubles * sizeof(double), 256);
-    const size_t off_ws = off; off = align_up(off + wsd * sizeof(double), 256);
-    const size_t off_scr = off; off = align_up(off + (size_t)grid * slot_bytes, 256);
-    const size_t total = off;
+    pc.off_inst = off; off = align_up(off + call.count * sizeof(InstDev), 256);
+    pc.off_work = off; off = align_up(off + nwork * sizeof(ChunkRef), 256);
+    pc.off_gl = off; off = align_up(off + gl_doubles * sizeof(double), 256);
+    pc.off_ck = off; off = align_up(off + ck_doubles * sizeof(double), 256);
+    pc.off_ws = off; off = align_up(off + wsd * sizeof(double), 256);
+    for (Segment& sg : pc.segs) {
+        const size_t slot_bytes = (size_t)sg.slot_elems * tsz;
+        const double share = (double)sg.nwork / (double)std::max<size_t>(nwork, 1);
+        const size_t seg_budget = std::max<size_t>(slot_bytes, (size_t)(budget * share));
+        int64_t grid = std::min<int64_t>(sg.nwork, (int64_t)pc.sms * 8);
+        grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)(seg_budget / std::max<size_t>(slot_bytes, 1))));
+        sg.grid = grid;
+        sg.scr_off = off;
+        off = align_up(off + (size_t)grid * slot_bytes, 256);
+    }
+    if (pc.any_carry) {
+        // the carry record runs the generic kernel over all instances
+        for (size_t i = 0; i < call.count; ++i) {
+            const mgb_problem& p = call.probs[i];
+            const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
+            pc.gslot_elems = std::max<int64_t>(pc.gslot_elems, (int64_t)(p.n + 4) * L * dv[i].m + 3 * (int64_t)p.n * dv[i].m);
+        }
+        const size_t slot_bytes = (size_t)pc.gslot_elems * tsz;
+        pc.ggrid = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>((int64_t)nwork, (int64_t)pc.sms * 8),
+                                                          (int64_t)(budget / std::max<size_t>(slot_bytes, 1))));
+        pc.off_gscr = off;
+        off = align_up(off + (size_t)pc.ggrid * slot_bytes, 256);
+    }
+    pc.bytes = off;
+    return MGB_OK;
+}
 
-    Workspace ws;
-    ws.st = call.stream;
-    MGB_CUDA_TRY(cudaMallocAsync(&ws.base, total, call.stream));
-    char* base = static_cast<char*>(ws.base);
-
-    // ---- host descriptors
-    std::vector<InstDev> hi(n_inst);
-    std::vector<ChunkRef> hw(nwork);
-    std::vector<double> hgl(gl_doubles);
-    size_t wpos = 0, glpos = 0, ckpos = 0, wspos = 0;
-    for (size_t i = 0; i < n_inst; ++i) {
+// Fill the host descriptors for a device buffer at `base`.
+void plan_fill(const Call& call, PlanCore& pc, const std::vector<Derived>& dv) {
+    auto gl = gl_snapshot();
+    char* base = pc.base;
+    pc.hi.assign(call.count, InstDev{});
+    pc.work.clear();
+    pc.work.reserve((size_t)pc.segs.back().work_off + (size_t)pc.segs.back().nwork);
+    pc.gl.clear();
+    size_t ckpos = 0, wspos = 0;
+    for (size_t k = 0; k < call.count; ++k) {
+        const int32_t i = pc.order[k];
         const mgb_problem& p = call.probs[i];
         const Derived& v = dv[i];
-        InstDev& I = hi[i];
+        InstDev& I = pc.hi[k];
         std::memset(&I, 0, sizeof(I));
         I.A = call.A[i];
-        if (!call.vjp) {
-            I.out = call.out[i];
-            I.carry = (call.carry && call.carry[i]) ? call.carry[i] : nullptr;
-        } else {
-            I.cot = call.cot[i];
-            I.dA = call.dA[i];
-        }
+        I.out = call.out ? call.out[i] : nullptr;
+        I.carry = (call.carry && call.carry[i]) ? call.carry[i] : nullptr;
+        I.cot = call.cot ? call.cot[i] : nullptr;
+        I.dA = call.dA ? call.dA[i] : nullptr;
         double* ck;
-        const bool user_ck = call.vjp ? (call.ckpt_in && call.ckpt_in[i]) : (call.ckpt_out && call.ckpt_out[i]);
-        if (user_ck) {
-            ck = static_cast<double*>(call.vjp ? const_cast<void*>(call.ckpt_in[i]) : call.ckpt_out[i]);
+        if (call.ckpt_in && call.ckpt_in[i]) {
+            ck = static_cast<double*>(const_cast<void*>(call.ckpt_in[i]));
+        } else if (call.ckpt_out && call.ckpt_out[i]) {
+            ck = static_cast<double*>(call.ckpt_out[i]);
         } else {
-            ck = reinterpret_cast<double*>(base + off_ck) + ckpos;
+            ck = reinterpret_cast<double*>(base + pc.off_ck) + ckpos;
             ckpos += ckpt_doubles(p, v);
         }
         I.pi = ck;
         I.lam = ck + (size_t)(v.C + 1) * v.nm;
-        double* w = reinterpret_cast<double*>(base + off_ws) + wspos;
+        double* w = reinterpret_cast<double*>(base + pc.off_ws) + wspos;
         wspos += ws_doubles(v);
         I.rho = w; w += (size_t)v.C * v.nm;
         I.dq = w; w += (size_t)v.Q * v.nm;
@@ -318,15 +416,12 @@ mgb_status run(const Call& call) {
         I.eb = w; w += v.nm;
         I.db = w; w += v.nm;
         I.tt = w; w += v.nm;
-        double* g = reinterpret_cast<double*>(base + off_gl) + glpos;
+        double* g = reinterpret_cast<double*>(base + pc.off_gl) + pc.gl.size();
         const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
-        for (int q = 0; q < v.Q; ++q) {
-            hgl[glpos + q] = gl->w[go + q];
-            hgl[glpos + v.Q + q] = gl->x[go + q];
-        }
+        for (int q = 0; q < v.Q; ++q) pc.gl.push_back(gl->w[go + q]);
+        for (int q = 0; q < v.Q; ++q) pc.gl.push_back(gl->x[go + q]);
         I.glw = g;
         I.glx = g + v.Q;
-        glpos += 2 * (size_t)v.Q;
         I.dt = (p.tf - p.t0) / (double)(p.samples - 1);
         I.dt_k = kernel_step(p, I.dt);
         I.sig = (I.dt_k != 0.0) ? I.dt / I.dt_k : 1.0;
@@ -338,46 +433,129 @@ mgb_status run(const Call& call) {
         I.Q = v.Q;
         I.K = v.K;
         I.op = p.op;
-        for (int c = 0; c < v.C; ++c) hw[wpos++] = ChunkRef{(int32_t)i, c};
+        for (int c = 0; c < v.C; ++c) pc.work.push_back(ChunkRef{(int32_t)k, c});
     }
-    InstDev* d_inst = reinterpret_cast<InstDev*>(base + off_inst);
-    ChunkRef* d_work = reinterpret_cast<ChunkRef*>(base + off_work);
-    MGB_CUDA_TRY(cudaMemcpyAsync(d_inst, hi.data(), n_inst * sizeof(InstDev), cudaMemcpyHostToDevice, call.stream));
-    MGB_CUDA_TRY(cudaMemcpyAsync(d_work, hw.data(), nwork * sizeof(ChunkRef), cudaMemcpyHostToDevice, call.stream));
-    MGB_CUDA_TRY(cudaMemcpyAsync(base + off_gl, hgl.data(), gl_doubles * sizeof(double), cudaMemcpyHostToDevice, call.stream));
-    // pageable copies above are staged before return; host vectors may go.
-    MGB_CUDA_TRY(cudaStreamSynchronize(call.stream));
-
-    LaunchArgs la;
-    la.insts = d_inst;
-    la.work = d_work;
-    la.nwork = (int64_t)nwork;
-    la.scratch = base + off_scr;
-    la.slot_elems = slot_elems;
-    la.grid = grid;
-    la.f64io = f64io;
-    la.stream = call.stream;
-    const int rule = p0.integrator;
-    const int cnt = (int)n_inst;
-
-    const bool need_fwd_scan = !call.vjp || !(call.ckpt_in);
-    bool all_ck_in = call.vjp && call.ckpt_in;
-    if (all_ck_in)
-        for (size_t i = 0; i < n_inst; ++i) all_ck_in = all_ck_in && call.ckpt_in[i];
-    if (!call.vjp || !all_ck_in) {
-        (void)need_fwd_scan;
-        MGB_CUDA_TRY(timed("chunk_local", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_LOCAL, la, hi, di.sms); }));
-        MGB_CUDA_TRY(timed("scan", call.stream, [&] { return launch_small(true, kind, SMALL_SCAN, d_inst, cnt, f64io, 0, call.stream); }));
+    for (Segment& sg : pc.segs) {
+        sg.hi.assign(pc.hi.begin() + sg.first, pc.hi.begin() + sg.first + sg.count);
+        sg.tc = TunedChoice{};
     }
-    MGB_CUDA_TRY(timed("fin_fwd", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_FWD, d_inst, cnt, f64io, call.vjp ? 0 : 1, call.stream); }));
-    if (!call.vjp) {
-        if (any_carry) MGB_CUDA_TRY(timed("chunk_carry", call.stream, [&] { return launch_generic_chunk(plain, kind, rule, MODE_CARRY, la); }));
+}
+
+mgb_status plan_upload(PlanCore& pc, cudaStream_t st, bool synchronous) {
+    char* base = pc.base;
+    if (synchronous) {
+        MGB_CUDA_TRY(cudaMemcpy(base + pc.off_inst, pc.hi.data(), pc.hi.size() * sizeof(InstDev), cudaMemcpyHostToDevice));
+        MGB_CUDA_TRY(cudaMemcpy(base + pc.off_work, pc.work.data(), pc.work.size() * sizeof(ChunkRef), cudaMemcpyHostToDevice));
+        MGB_CUDA_TRY(cudaMemcpy(base + pc.off_gl, pc.gl.data(), pc.gl.size() * sizeof(double), cudaMemcpyHostToDevice));
     } else {
-        MGB_CUDA_TRY(timed("fin_vjp", call.stream, [&] { return launch_small(true, kind, SMALL_FIN_VJP, d_inst, cnt, f64io, 0, call.stream); }));
-        MGB_CUDA_TRY(timed("rscan", call.stream, [&] { return launch_small(true, kind, SMALL_RSCAN, d_inst, cnt, f64io, 0, call.stream); }));
-        MGB_CUDA_TRY(timed("chunk_vjp", call.stream, [&] { return launch_chunk_any(plain, kind, rule, MODE_VJP, la, hi, di.sms); }));
+        MGB_CUDA_TRY(cudaMemcpyAsync(base + pc.off_inst, pc.hi.data(), pc.hi.size() * sizeof(InstDev), cudaMemcpyHostToDevice, st));
+        MGB_CUDA_TRY(cudaMemcpyAsync(base + pc.off_work, pc.work.data(), pc.work.size() * sizeof(ChunkRef), cudaMemcpyHostToDevice, st));
+        MGB_CUDA_TRY(cudaMemcpyAsync(base + pc.off_gl, pc.gl.data(), pc.gl.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        MGB_CUDA_TRY(cudaStreamSynchronize(st));  // the host vectors may change after this
     }
     return MGB_OK;
+}
+
+mgb_status plan_streams(PlanCore& pc) {
+    for (const Segment& sg : pc.segs)
+        for (int mode : {MODE_LOCAL, MODE_VJP})
+            MGB_CUDA_TRY(prepare_tuned(choose_tuned(pc.plain, pc.kind, pc.rule, mode, pc.f64io != 0, sg.hi), pc.rule, mode));
+    if (pc.segs.size() < 2 || pc.fork) return MGB_OK;
+    MGB_CUDA_TRY(cudaEventCreateWithFlags(&pc.fork, cudaEventDisableTiming));
+    for (Segment& sg : pc.segs) {
+        MGB_CUDA_TRY(cudaStreamCreateWithFlags(&sg.stream, cudaStreamNonBlocking));
+        MGB_CUDA_TRY(cudaEventCreateWithFlags(&sg.done, cudaEventDisableTiming));
+    }
+    return MGB_OK;
+}
+
+LaunchArgs seg_args(const PlanCore& pc, const Segment& sg, cudaStream_t st) {
+    LaunchArgs la;
+    la.insts = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst);
+    la.work = reinterpret_cast<const ChunkRef*>(pc.base + pc.off_work) + sg.work_off;
+    la.nwork = sg.nwork;
+    la.scratch = pc.base + sg.scr_off;
+    la.slot_elems = sg.slot_elems;
+    la.grid = sg.grid;
+    la.f64io = pc.f64io;
+    la.stream = st;
+    return la;
+}
+
+// Chunk kernel of every segment, concurrently when there are several.
+mgb_status plan_chunks(PlanCore& pc, int mode, cudaStream_t st, const char* name) {
+    if (pc.segs.size() == 1) {
+        Segment& sg = pc.segs[0];
+        const LaunchArgs la = seg_args(pc, sg, st);
+        MGB_CUDA_TRY(timed(name, st, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
+        return MGB_OK;
+    }
+    MGB_CUDA_TRY(cudaEventRecord(pc.fork, st));
+    for (Segment& sg : pc.segs) {
+        MGB_CUDA_TRY(cudaStreamWaitEvent(sg.stream, pc.fork, 0));
+        const LaunchArgs la = seg_args(pc, sg, sg.stream);
+        MGB_CUDA_TRY(timed(name, sg.stream, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
+        MGB_CUDA_TRY(cudaEventRecord(sg.done, sg.stream));
+    }
+    for (Segment& sg : pc.segs) MGB_CUDA_TRY(cudaStreamWaitEvent(st, sg.done, 0));
+    return MGB_OK;
+}
+
+mgb_status plan_forward(PlanCore& pc, cudaStream_t st) {
+    if (!pc.has_out) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+    const InstDev* d_inst = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst);
+    const int cnt = (int)pc.count;
+    mgb_status s = plan_chunks(pc, MODE_LOCAL, st, "chunk_local");
+    if (s != MGB_OK) return s;
+    MGB_CUDA_TRY(timed("scan", st, [&] { return launch_small(true, pc.kind, SMALL_SCAN, d_inst, cnt, pc.f64io, 0, st); }));
+    MGB_CUDA_TRY(timed("fin_fwd", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_FWD, d_inst, cnt, pc.f64io, 1, st); }));
+    if (pc.any_carry) {
+        LaunchArgs la;
+        la.insts = d_inst;
+        la.work = reinterpret_cast<const ChunkRef*>(pc.base + pc.off_work);
+        la.nwork = (int64_t)pc.work.size();
+        la.scratch = pc.base + pc.off_gscr;
+        la.slot_elems = pc.gslot_elems;
+        la.grid = pc.ggrid;
+        la.f64io = pc.f64io;
+        la.stream = st;
+        MGB_CUDA_TRY(timed("chunk_carry", st, [&] { return launch_generic_chunk(pc.plain, pc.kind, pc.rule, MODE_CARRY, la); }));
+    }
+    return MGB_OK;
+}
+
+mgb_status plan_vjp(PlanCore& pc, cudaStream_t st, bool recompute) {
+    if (!pc.has_vjp) return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent and dA buffers were not given to this plan");
+    const InstDev* d_inst = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst);
+    const int cnt = (int)pc.count;
+    if (recompute) {
+        mgb_status s = plan_chunks(pc, MODE_LOCAL, st, "chunk_local");
+        if (s != MGB_OK) return s;
+        MGB_CUDA_TRY(timed("scan", st, [&] { return launch_small(true, pc.kind, SMALL_SCAN, d_inst, cnt, pc.f64io, 0, st); }));
+    }
+    MGB_CUDA_TRY(timed("fin_fwd", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_FWD, d_inst, cnt, pc.f64io, 0, st); }));
+    MGB_CUDA_TRY(timed("fin_vjp", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_VJP, d_inst, cnt, pc.f64io, 0, st); }));
+    MGB_CUDA_TRY(timed("rscan", st, [&] { return launch_small(true, pc.kind, SMALL_RSCAN, d_inst, cnt, pc.f64io, 0, st); }));
+    return plan_chunks(pc, MODE_VJP, st, "chunk_vjp");
+}
+
+// One-shot call: plan in stream-ordered memory, run, release.
+mgb_status run(const Call& call) {
+    if (call.count == 0) return MGB_OK;
+    PlanCore pc;
+    std::vector<Derived> dv;
+    mgb_status st = plan_layout(call, pc, dv);
+    if (st != MGB_OK) return st;
+    Workspace ws;
+    ws.st = call.stream;
+    MGB_CUDA_TRY(cudaMallocAsync(&ws.base, pc.bytes, call.stream));
+    pc.base = static_cast<char*>(ws.base);
+    plan_fill(call, pc, dv);
+    st = plan_upload(pc, call.stream, false);
+    if (st == MGB_OK) st = plan_streams(pc);
+    if (st == MGB_OK) st = call.vjp ? plan_vjp(pc, call.stream, !pc.all_ck_in) : plan_forward(pc, call.stream);
+    pc.release_streams();
+    return st;
 }
 
 }  // namespace
@@ -396,7 +574,75 @@ cudaError_t launch_chunk_any(bool plain, int kind, int rule, int mode, const Lau
 // ============================================================================
 // C ABI
 // ============================================================================
+struct mgb_plan {
+    PlanCore pc;
+    bool forward_done = false;
+};
+
 extern "C" {
+
+mgb_status mgb_plan_create(const mgb_problem* probs, size_t count, const void* const* A, void* const* out,
+                           const void* const* cot, void* const* dA, mgb_plan** plan) {
+    g_last_error.clear();
+    if (!plan) return fail(MGB_ERR_INVALID_ARGUMENT, "plan pointer must not be null");
+    *plan = nullptr;
+    Call c{};
+    c.count = count;
+    c.probs = probs;
+    c.A = A;
+    c.out = out;
+    c.cot = cot;
+    c.dA = dA;
+    std::unique_ptr<mgb_plan> P(new mgb_plan());
+    std::vector<Derived> dv;
+    mgb_status st = plan_layout(c, P->pc, dv);
+    if (st != MGB_OK) return st;
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, P->pc.bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? MGB_ERR_OUT_OF_MEMORY : MGB_ERR_CUDA,
+                    std::string("plan workspace: ") + cudaGetErrorString(e));
+    }
+    P->pc.base = static_cast<char*>(base);
+    plan_fill(c, P->pc, dv);
+    st = plan_upload(P->pc, nullptr, true);
+    if (st == MGB_OK) st = plan_streams(P->pc);
+    if (st != MGB_OK) {
+        P->pc.release_streams();
+        cudaFree(base);
+        return st;
+    }
+    *plan = P.release();
+    return MGB_OK;
+}
+
+mgb_status mgb_plan_forward(mgb_plan* plan, void* stream) {
+    g_last_error.clear();
+    if (!plan) return fail(MGB_ERR_INVALID_ARGUMENT, "plan must not be null");
+    mgb_status st = plan_forward(plan->pc, static_cast<cudaStream_t>(stream));
+    if (st == MGB_OK) plan->forward_done = true;
+    return st;
+}
+
+mgb_status mgb_plan_vjp(mgb_plan* plan, void* stream) {
+    g_last_error.clear();
+    if (!plan) return fail(MGB_ERR_INVALID_ARGUMENT, "plan must not be null");
+    return plan_vjp(plan->pc, static_cast<cudaStream_t>(stream), !plan->forward_done);
+}
+
+size_t mgb_plan_bytes(const mgb_plan* plan) { return plan ? plan->pc.bytes : 0; }
+
+mgb_status mgb_plan_destroy(mgb_plan* plan) {
+    g_last_error.clear();
+    if (!plan) return MGB_OK;
+    plan->pc.release_streams();
+    cudaError_t e = plan->pc.base ? cudaFree(plan->pc.base) : cudaSuccess;
+    delete plan;
+    if (e != cudaSuccess) return fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+    return MGB_OK;
+}
+
 
 mgb_status mgb_forward(const mgb_problem* p, const void* A, void* out, void* carry, void* ckpt, void* stream) {
     g_last_error.clear();

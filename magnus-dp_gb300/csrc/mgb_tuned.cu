@@ -14,6 +14,7 @@
 // values of levels 1..n-1 to a per-CTA tape in global memory, then runs the
 // adjoint over the groups in reverse order with dA accumulated in registers.
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include "mgb_common.cuh"
@@ -384,14 +385,42 @@ size_t tile_smem_bytes(int) {
     return (size_t)TileCfg<D>::OPND * sizeof(float);
 }
 
+// The dynamic shared-memory opt-in is a per-kernel, per-device setting; it is
+// made once (and can be made ahead of a stream capture by prepare_tuned).
+template <int D, int RULE, int MODE>
+cudaError_t set_tile_attr() {
+    static std::mutex mu;
+    static std::vector<bool> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, false);
+    if (done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_tile<D, RULE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tile_smem_bytes<D>(0));
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
+}
+
 template <int D, int RULE, int MODE>
 cudaError_t launch_tile_t(const LaunchArgs& a, int nmax, int grid) {
     const size_t smem = tile_smem_bytes<D>(nmax);
-    cudaError_t e = cudaFuncSetAttribute(k_tile<D, RULE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = set_tile_attr<D, RULE, MODE>();
     if (e != cudaSuccess) return e;
     k_tile<D, RULE, MODE><<<grid, TNT, smem, a.stream>>>(a.insts, a.work, a.nwork, static_cast<float*>(a.scratch),
                                                         a.slot_elems);
     return cudaGetLastError();
+}
+
+template <int D, int MODE>
+cudaError_t set_tile_attr_r(int rule) {
+    switch (rule) {
+        case R_BOOLE: return set_tile_attr<D, R_BOOLE, MODE>();
+        case R_SIMPSON: return set_tile_attr<D, R_SIMPSON, MODE>();
+        case R_TRAP: return set_tile_attr<D, R_TRAP, MODE>();
+        default: return set_tile_attr<D, R_RIEMANN, MODE>();
+    }
 }
 
 template <int D, int MODE>
@@ -428,6 +457,12 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     tc.nmax = nmax;
     tc.ctas_per_sm = smem <= 113 * 1024 ? 2 : 1;
     return tc;
+}
+
+cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode) {
+    if (!tc.use) return cudaSuccess;
+    if (tc.D == 32) return mode == MODE_LOCAL ? set_tile_attr_r<32, MODE_LOCAL>(rule) : set_tile_attr_r<32, MODE_VJP>(rule);
+    return mode == MODE_LOCAL ? set_tile_attr_r<16, MODE_LOCAL>(rule) : set_tile_attr_r<16, MODE_VJP>(rule);
 }
 
 cudaError_t launch_tuned(const TunedChoice& tc, bool, int, int rule, int mode, const LaunchArgs& a, int sms) {

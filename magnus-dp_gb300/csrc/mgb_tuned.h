@@ -17,6 +17,7 @@ struct TunedChoice {
 };
 
 TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi);
+cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode);
 cudaError_t launch_tuned(const TunedChoice& tc, bool plain, int kind, int rule, int mode, const LaunchArgs& a, int sms);
 cudaError_t launch_chunk_any(bool plain, int kind, int rule, int mode, const LaunchArgs& a,
                              const std::vector<InstDev>& hi, int sms);

@@ -64,6 +64,11 @@ SIGNATURES = {
     "mgb_last_error": (ctypes.c_char_p, []),
     "mgb_version": (ctypes.c_int, []),
     "mgb_forward_noalloc": (ctypes.c_int, [_PP, _VP, _VP, _VP]),
+    "mgb_plan_create": (ctypes.c_int, [_PP, ctypes.c_size_t, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_void_p)]),
+    "mgb_plan_forward": (ctypes.c_int, [_VP, _VP]),
+    "mgb_plan_vjp": (ctypes.c_int, [_VP, _VP]),
+    "mgb_plan_bytes": (ctypes.c_size_t, [_VP]),
+    "mgb_plan_destroy": (ctypes.c_int, [_VP]),
     "mgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "mgb_profile_read": (ctypes.c_size_t, [ctypes.POINTER(KernelTime), ctypes.c_size_t, ctypes.c_int]),
 }
