@@ -216,41 +216,45 @@ def main():
     prob = _lib.make_problem(kind=_lib.KIND_MATRIX, dtype_code=_lib.DTYPE_F32, precision=prec, op=_lib.OP_SUM,
                              integrator=_lib.INTEGRATOR_CODES[c["integrator"]], n=n, samples=S, dim=d, t0=c["t0"],
                              tf=c["tf"], checkpoint_K=c["K"])
-    ck_bytes = lib.mgb_checkpoint_bytes(ctypes.byref(prob))
-    ck = torch.empty((B, ck_bytes), dtype=torch.uint8, device=dev)
     probs = (_lib.Problem * B)(*([prob] * B))
 
     def ptrs(t):
         return (ctypes.c_void_p * B)(*[t[i].data_ptr() for i in range(B)])
 
-    pA, pO, pC, pG, pD = ptrs(A), ptrs(out), ptrs(ck), ptrs(cot), ptrs(dA)
+    # One plan binds the batch's buffers (and holds the chunk checkpoints);
+    # a step = plan forward + plan VJP, captured once into a CUDA graph.
+    plan = ctypes.c_void_p()
+    _lib.check(lib.mgb_plan_create(probs, B, ptrs(A), ptrs(out), ptrs(cot), ptrs(dA), ctypes.byref(plan)))
     stream = torch.cuda.current_stream(dev)
     sptr = ctypes.c_void_p(stream.cuda_stream)
 
-    def step():
-        _lib.check(lib.mgb_forward_batched(probs, B, pA, pO, pC, sptr))
-        _lib.check(lib.mgb_vjp_batched(probs, B, pA, pG, pC, pD, sptr))
+    def step_eager():
+        _lib.check(lib.mgb_plan_forward(plan, sptr))
+        _lib.check(lib.mgb_plan_vjp(plan, sptr))
 
+    step_eager()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        gs = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        _lib.check(lib.mgb_plan_forward(plan, gs))
+        _lib.check(lib.mgb_plan_vjp(plan, gs))
     for _ in range(max(args.warmup, 3)):
-        step()
+        graph.replay()
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
     clocks.start()
-    lib.mgb_profile_enable(1)
-    _lib.profile_read(reset=True)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(args.steps):
-        step()
+        graph.replay()
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    lib.mgb_profile_enable(0)
-    kernels = _lib.profile_read(reset=True)
     clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
     ms_t = torch.tensor([ms], device=dev)
@@ -258,7 +262,17 @@ def main():
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
     ms = float(ms_t.item())
     value = world * B * S * n / (ms / 1e3)
-    launches = sum(v[0] for v in kernels.values())
+
+    # per-kernel CUDA-event times: the same steps run eagerly with the
+    # library's launch timing enabled (events bracket every kernel launch)
+    lib.mgb_profile_enable(1)
+    _lib.profile_read(reset=True)
+    for _ in range(args.steps):
+        step_eager()
+    torch.cuda.synchronize()
+    lib.mgb_profile_enable(0)
+    kernels = _lib.profile_read(reset=True)
+    launches = sum(v[0] for v in kernels.values()) // args.steps * args.steps
 
     # ---- roofline of the dominant kernel
     hbm_peak, bf16_peak, sm_max, peak_src = load_peaks()
@@ -288,7 +302,8 @@ def main():
               "config": {"workload": f"config4: {B} x d={d} A(t)=C0+C1 t+C2 t^2+C3 cos5t, S={S}, Boole, n={n}, "
                                      f"sum, float32 in, fwd+VJP, checkpoints every {c['K']} samples",
                          "precision": args.precision, "global_batch": B * world,
-                         "cache": "inputs 68.7 GB >> L2 (no flush needed)"},
+                         "cache": "inputs 68.7 GB >> L2 (no flush needed)",
+                         "execution": "mgb_plan forward+VJP captured in one CUDA graph, replayed per step"},
               "roofline": roof, "gpu_launches": launches, "clocks": clk,
               "kernels_ms_per_step": {k: v[1] / args.steps for k, v in kernels.items()}}
 
@@ -331,6 +346,9 @@ def main():
         cot_host = cot[:eb].cpu().pin_memory()
         dA_host = torch.empty_like(A_host).pin_memory()
         out_host = torch.empty((eb, d, d), dtype=torch.float32).pin_memory()
+        del graph
+        _lib.check(lib.mgb_plan_destroy(plan))
+        plan = None
         del dA
         torch.cuda.empty_cache()
         A_dev = torch.empty((eb, S, d, d), dtype=torch.float32, device=dev)
@@ -369,6 +387,8 @@ def main():
         result["cpu_baseline"] = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": f"{inst} config4 trajectories at S={args.cpu_samples} (of 32769), "
                                             f"fwd + VJP, float32, {cpu_s:.1f} s"}
+    if plan is not None and plan.value:
+        _lib.check(lib.mgb_plan_destroy(plan))
     if rank == 0:
         print(json.dumps(result))
     if world > 1:

@@ -441,6 +441,15 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     if (plain || f64io || kind != KIND_MATRIX || hi.empty()) return tc;
     if (mode != MODE_LOCAL && mode != MODE_VJP) return tc;
     const int D = hi[0].d;
+    if (D == 64 || D == 128) {
+        for (const InstDev& I : hi)
+            if (I.d != D || reinterpret_cast<uintptr_t>(I.A) % 16 != 0) return tc;
+        tc.use = true;
+        tc.family = 3;
+        tc.D = D;
+        tc.ctas_per_sm = D == 64 ? 2 : 1;
+        return tc;
+    }
     if (D != 16 && D != 32) return tc;
     int nmax = 0;
     for (const InstDev& I : hi) {
@@ -461,11 +470,16 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
 
 cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode) {
     if (!tc.use) return cudaSuccess;
+    if (tc.family == 3) {
+        LaunchArgs none{};
+        return launch_big(tc.D, rule, mode, none, 1, true);
+    }
     if (tc.D == 32) return mode == MODE_LOCAL ? set_tile_attr_r<32, MODE_LOCAL>(rule) : set_tile_attr_r<32, MODE_VJP>(rule);
     return mode == MODE_LOCAL ? set_tile_attr_r<16, MODE_LOCAL>(rule) : set_tile_attr_r<16, MODE_VJP>(rule);
 }
 
 cudaError_t launch_tuned(const TunedChoice& tc, bool, int, int rule, int mode, const LaunchArgs& a, int sms) {
+    if (tc.family == 3) return launch_big(tc.D, rule, mode, a, sms * tc.ctas_per_sm, false);
     int grid = (int)std::min<int64_t>(a.grid, (int64_t)sms * tc.ctas_per_sm);
     if (grid < 1) grid = 1;
     if (tc.D == 32)

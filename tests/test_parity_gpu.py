@@ -237,3 +237,23 @@ def test_tiled_kernel_orders(n, cuda):
     gref = O.vjp(A.astype(np.float64), cot.astype(np.float64), n, 0.0, 1.0, "sum", "Boole")
     g = core.compute_vjp(n, A, cot, integrator="Boole", precision="mixed", checkpoint_K=16)
     assert rel(g, gref) <= 1e-6, rel(g, gref)
+
+
+@pytest.mark.parametrize("integrator,S", [("Boole", 129), ("Simpson", 131), ("Trapezoid", 97), ("Riemann", 90)])
+@pytest.mark.parametrize("d", [64, 128])
+def test_big_mixed_kernel_float32(integrator, S, d, cuda):
+    """float32 inputs at d = 64 / 128 in mixed precision run the level-major
+    shared-memory tiled kernel (mgb_big.cu); orders and VJP within 1e-6."""
+    A = smooth_samples(S, d, seed=d + 5).astype(np.float32)
+    A64 = A.astype(np.float64)
+    n = 4
+    ref = O.forward(A64, n, 0.0, 1.0, "many", integrator)
+    out = core.compute(n, A, 0.0, 1.0, op="many", integrator=integrator, precision="mixed", checkpoint_K=32)
+    for k in range(n):
+        assert rel(out[k], ref[k]) <= 1e-6, (k, rel(out[k], ref[k]))
+    rng = np.random.default_rng(d)
+    cot = rng.standard_normal((d, d)).astype(np.float32)
+    gref = O.vjp(A64, cot.astype(np.float64), n, 0.0, 1.0, "sum", integrator)
+    g = core.compute_vjp(n, A, cot, t0=0.0, tf=1.0, op="sum", integrator=integrator, precision="mixed",
+                         checkpoint_K=32)
+    assert rel(g, gref) <= 1e-6, rel(g, gref)
