@@ -334,8 +334,15 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
             const int32_t i = pc.order[k];
             const mgb_problem& p = call.probs[i];
             sg.nwork += dv[i].C;
-            const int64_t L = std::min<int64_t>((int64_t)dv[i].K, (int64_t)p.samples - 1) + 1;
-            sg.slot_elems = std::max<int64_t>(sg.slot_elems, (int64_t)(p.n + 4) * L * dv[i].m + 3 * (int64_t)p.n * dv[i].m);
+            InstDev I{};  // the fields the kernel choice looks at
+            I.A = call.A[i];
+            I.dA = call.dA ? call.dA[i] : nullptr;
+            I.S = (int64_t)p.samples;
+            I.d = (p.kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p.dim;
+            I.m = dv[i].m;
+            I.n = (int32_t)p.n;
+            I.K = dv[i].K;
+            sg.hi.push_back(I);
         }
         wpos += sg.nwork;
         pc.segs.push_back(std::move(sg));
@@ -349,14 +356,13 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     pc.off_ck = off; off = align_up(off + ck_doubles * sizeof(double), 256);
     pc.off_ws = off; off = align_up(off + wsd * sizeof(double), 256);
     for (Segment& sg : pc.segs) {
-        const size_t slot_bytes = (size_t)sg.slot_elems * tsz;
         const double share = (double)sg.nwork / (double)std::max<size_t>(nwork, 1);
-        const size_t seg_budget = std::max<size_t>(slot_bytes, (size_t)(budget * share));
-        int64_t grid = std::min<int64_t>(sg.nwork, (int64_t)pc.sms * 8);
-        grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)(seg_budget / std::max<size_t>(slot_bytes, 1))));
-        sg.grid = grid;
+        const size_t seg_budget = std::max<size_t>((size_t)64 << 20, (size_t)(budget * share));
+        const SegSizing sz = size_segment(pc.plain, pc.kind, pc.rule, pc.f64io != 0, sg.hi, sg.nwork, pc.sms, seg_budget);
+        sg.slot_elems = sz.slot_elems;
+        sg.grid = sz.grid;
         sg.scr_off = off;
-        off = align_up(off + (size_t)grid * slot_bytes, 256);
+        off = align_up(off + (size_t)sz.grid * (size_t)sz.slot_elems * tsz, 256);
     }
     if (pc.any_carry) {
         // the carry record runs the generic kernel over all instances

@@ -438,8 +438,18 @@ cudaError_t launch_tile_r(int rule, const LaunchArgs& a, int nmax, int grid) {
 TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi) {
     TunedChoice tc;
     (void)rule;
-    if (plain || f64io || kind != KIND_MATRIX || hi.empty()) return tc;
-    if (mode != MODE_LOCAL && mode != MODE_VJP) return tc;
+    if (hi.empty() || (mode != MODE_LOCAL && mode != MODE_VJP)) return tc;
+    if (hi[0].m == 4) {  // 2x2 matrices and SpaceCurve: thread-per-chunk, both precisions
+        for (const InstDev& I : hi) {
+            if (I.m != 4 || I.n > small_family_max_levels()) return tc;
+            if (kind == KIND_MATRIX && reinterpret_cast<uintptr_t>(I.A) % 16 != 0) return tc;
+        }
+        tc.use = true;
+        tc.family = 1;
+        tc.D = 2;
+        return tc;
+    }
+    if (plain || f64io || kind != KIND_MATRIX) return tc;
     const int D = hi[0].d;
     if (D == 64 || D == 128) {
         for (const InstDev& I : hi)
@@ -478,7 +488,32 @@ cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode) {
     return mode == MODE_LOCAL ? set_tile_attr_r<16, MODE_LOCAL>(rule) : set_tile_attr_r<16, MODE_VJP>(rule);
 }
 
-cudaError_t launch_tuned(const TunedChoice& tc, bool, int, int rule, int mode, const LaunchArgs& a, int sms) {
+SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::vector<InstDev>& hi, int64_t nwork,
+                       int sms, size_t budget_bytes) {
+    SegSizing sz;
+    const size_t tsz = plain ? sizeof(double) : sizeof(float);
+    int64_t Lmax = 1, generic = 0;
+    for (const InstDev& I : hi) {
+        const int64_t L = std::min<int64_t>((int64_t)I.K, I.S - 1) + 1;
+        Lmax = std::max(Lmax, L);
+        generic = std::max<int64_t>(generic, (int64_t)(I.n + 4) * L * I.m + 3 * (int64_t)I.n * I.m);
+    }
+    TunedChoice tc = choose_tuned(plain, kind, rule, MODE_VJP, f64io, hi);
+    int64_t want;
+    if (tc.use && tc.family == 1) {
+        sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4;  // one thread's tape
+        want = std::min<int64_t>(nwork, (int64_t)sms * 1024);
+    } else {
+        sz.slot_elems = generic;
+        want = std::min<int64_t>(nwork, (int64_t)sms * 8);
+    }
+    const size_t slot_bytes = (size_t)sz.slot_elems * tsz;
+    sz.grid = std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)(budget_bytes / std::max<size_t>(slot_bytes, 1))));
+    return sz;
+}
+
+cudaError_t launch_tuned(const TunedChoice& tc, bool plain, int kind, int rule, int mode, const LaunchArgs& a, int sms) {
+    if (tc.family == 1) return launch_small_family(plain, kind, rule, mode, a);
     if (tc.family == 3) return launch_big(tc.D, rule, mode, a, sms * tc.ctas_per_sm, false);
     int grid = (int)std::min<int64_t>(a.grid, (int64_t)sms * tc.ctas_per_sm);
     if (grid < 1) grid = 1;

@@ -10,11 +10,22 @@ namespace mgb {
 
 struct TunedChoice {
     bool use = false;
-    int family = 0;  // 2: group-tiled CTA kernel (mixed, d = 16 / 32); 3: level-major tiled (mixed, d = 64 / 128)
+    int family = 0;  // 1: thread-per-chunk registers (d = 2, SpaceCurve); 2: group-tiled CTA kernel (mixed, d = 16 / 32); 3: level-major tiled (mixed, d = 64 / 128)
     int D = 0;
     int nmax = 0;
     int ctas_per_sm = 1;
 };
+
+// Scratch geometry of a segment: per-slot elements (compute type) and the
+// number of slots (CTAs, or threads for the thread-per-chunk family).
+struct SegSizing {
+    int64_t slot_elems = 0;
+    int64_t grid = 0;
+};
+SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::vector<InstDev>& hi, int64_t nwork,
+                       int sms, size_t budget_bytes);
+cudaError_t launch_small_family(bool plain, int kind, int rule, int mode, const LaunchArgs& a);
+int small_family_max_levels();
 
 TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi);
 cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, bool prepare_only);
