@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--cpu-instances", type=int, default=0, help="0 = one per host thread")
     ap.add_argument("--cpu-samples", type=int, default=4097)
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/cpu legs (quick runs)")
+    ap.add_argument("--workload", default="config4", choices=["config4", "config1", "config2", "config3"],
+                    help="config4 = the headline fwd+VJP line; the others print their own measurement lines")
+    ap.add_argument("--instances", type=int, default=0, help="config3: number of instances (0 = all 10000)")
     return ap.parse_args()
 
 
@@ -178,11 +181,232 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- other configurations
+def _plan(lib, _lib, probs, A, out, cot=None, dA=None):
+    import ctypes as ct
+    B = len(probs)
+    P = (_lib.Problem * B)(*probs)
+
+    def ptrs(ts):
+        return None if ts is None else (ct.c_void_p * B)(*[t.data_ptr() for t in ts])
+
+    plan = ct.c_void_p()
+    _lib.check(lib.mgb_plan_create(P, B, ptrs(A), ptrs(out), ptrs(cot), ptrs(dA), ct.byref(plan)))
+    return plan
+
+
+def _time_graph(torch, fn, steps, warmup=3):
+    fn()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    for _ in range(warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    del g
+    return e0.elapsed_time(e1) / steps
+
+
+def _order_errors(mixed, plain):
+    """Per-order relative Frobenius error; orders that vanish (< 1e-6 of the
+    largest) are measured against the largest order's norm."""
+    mixed = np.asarray(mixed, dtype=np.float64)
+    plain = np.asarray(plain, dtype=np.float64)
+    scale = max(np.linalg.norm(plain[..., k, :]) for k in range(plain.shape[-2]))
+    errs = []
+    for k in range(plain.shape[-2]):
+        nk = np.linalg.norm(plain[..., k, :])
+        den = nk if nk >= 1e-6 * scale else scale
+        errs.append(float(np.linalg.norm(mixed[..., k, :] - plain[..., k, :]) / den))
+    return errs
+
+
+def run_config1(args):
+    """4096 SpaceCurves, S=65537 on [0,2], Simpson, n=6, op=many, float32,
+    forward (mixed) — HBM-bound on the 3-vector samples."""
+    import ctypes as ct
+    import torch
+    from magnus_gb300 import _lib, workloads
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    B, S, n = (args.batch if args.batch != CONFIG4["batch"] else 4096), 65537, 6
+    a, b = workloads.config1_coeffs(seed=1, batch=B)
+    F = workloads.config1_samples_torch(a, b, samples=S, device=dev)
+    out = torch.empty((B, n, 3), dtype=torch.float32, device=dev)
+    mk = lambda prec: _lib.make_problem(kind=_lib.KIND_SPACECURVE, dtype_code=_lib.DTYPE_F32, precision=prec,  # noqa
+                                        op=_lib.OP_MANY, integrator=1, n=n, samples=S, dim=2, t0=0.0, tf=2.0)
+    plan = _plan(lib, _lib, [mk(_lib.PRECISION_MIXED)] * B, [F[i] for i in range(B)], [out[i] for i in range(B)])
+    st = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ms = _time_graph(torch, lambda: _lib.check(lib.mgb_plan_forward(plan, ct.c_void_p(torch.cuda.current_stream().cuda_stream))), args.steps)
+    lib.mgb_plan_destroy(plan)
+    sub = 16
+    out_p = torch.empty((sub, n, 3), dtype=torch.float32, device=dev)
+    plan_p = _plan(lib, _lib, [mk(_lib.PRECISION_PLAIN)] * sub, [F[i] for i in range(sub)], [out_p[i] for i in range(sub)])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _lib.check(lib.mgb_plan_forward(plan_p, st))
+    e0.record()
+    _lib.check(lib.mgb_plan_forward(plan_p, st))
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    lib.mgb_plan_destroy(plan_p)
+    errs = _order_errors(out[:sub].cpu().numpy(), out_p.cpu().numpy())
+    bytes_alg = B * S * 3 * 4 + B * n * 3 * 4
+    gbs = bytes_alg / (ms / 1e3) / 1e9
+    hbm_peak = load_peaks()[0]
+    print(json.dumps({"workload": "config1: 4096 SpaceCurves, S=65537, Simpson, n=6, many, float32, forward",
+                      "metric": "samples·order/s forward", "value": B * S * n / (ms / 1e3), "ms": ms,
+                      "precision": "mixed", "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak,
+                                                         "unit": "GB/s", "frac": gbs / hbm_peak},
+                      "plain_fp64": {"value": sub * S * n / (plain_ms / 1e3), "instances": sub},
+                      "rel_err_per_order_vs_fp64": errs}))
+
+
+def run_config2(args):
+    """256 skew-symmetric d=64 A(t), S=16385, Boole, n=4, op=sum, float32,
+    forward (mixed) — FP32-products-bound."""
+    import ctypes as ct
+    import torch
+    from magnus_gb300 import _lib, workloads
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    B, S, n, d = (args.batch if args.batch != CONFIG4["batch"] else 256), 16385, 4, 64
+    Sk = workloads.config2_coeffs(seed=2, batch=B, d=d)
+    A = workloads.config2_samples_torch(Sk, samples=S, device=dev)
+    out = torch.empty((B, d, d), dtype=torch.float32, device=dev)
+    mk = lambda prec, op: _lib.make_problem(kind=0, dtype_code=_lib.DTYPE_F32, precision=prec, op=op,  # noqa
+                                            integrator=0, n=n, samples=S, dim=d, t0=0.0, tf=1.0)
+    plan = _plan(lib, _lib, [mk(_lib.PRECISION_MIXED, _lib.OP_SUM)] * B, [A[i] for i in range(B)],
+                 [out[i] for i in range(B)])
+    ms = _time_graph(torch, lambda: _lib.check(lib.mgb_plan_forward(plan, ct.c_void_p(torch.cuda.current_stream().cuda_stream))), args.steps)
+    lib.mgb_plan_destroy(plan)
+    sub = 4
+    st = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+    res = {}
+    for prec in (_lib.PRECISION_MIXED, _lib.PRECISION_PLAIN):
+        o = torch.empty((sub, n, d, d), dtype=torch.float32, device=dev)
+        pl = _plan(lib, _lib, [mk(prec, _lib.OP_MANY)] * sub, [A[i] for i in range(sub)], [o[i] for i in range(sub)])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        _lib.check(lib.mgb_plan_forward(pl, st))
+        e0.record()
+        _lib.check(lib.mgb_plan_forward(pl, st))
+        e1.record()
+        torch.cuda.synchronize()
+        res[prec] = (o.cpu().numpy().reshape(sub, n, d * d), e0.elapsed_time(e1))
+        lib.mgb_plan_destroy(pl)
+    errs = _order_errors(res[_lib.PRECISION_MIXED][0], res[_lib.PRECISION_PLAIN][0])
+    flops = (n - 1) * 2.0 * d ** 3 * S * B
+    tf = flops / (ms / 1e3) / 1e12
+    fp32_peak = 152 * 128 * 2 * load_peaks()[2] * 1e6 / 1e12
+    print(json.dumps({"workload": "config2: 256 x d=64 skew A(t), S=16385, Boole, n=4, sum, float32, forward",
+                      "metric": "samples·order/s forward", "value": B * S * n / (ms / 1e3), "ms": ms,
+                      "precision": "mixed", "fp32_simt": {"achieved_tflops": tf, "nominal_peak_tflops": fp32_peak,
+                                                          "frac": tf / fp32_peak},
+                      "plain_fp64": {"value": sub * S * n / (res[_lib.PRECISION_PLAIN][1] / 1e3), "instances": sub},
+                      "rel_err_per_order_vs_fp64": errs}))
+
+
+def run_config3(args):
+    """Uneven batch: d in {2..128}, S log-uniform in [257, 65537], n in 2..6,
+    A as config0 at each d, float32; fwd+VJP in mixed precision.  The float32
+    samples of all 10000 instances (~1.5 TB) exceed HBM, so instances run in
+    waves of <= 48 GB; each wave is one plan (instances grouped by dimension,
+    segments on concurrent streams) captured in a CUDA graph; sample
+    generation between waves is outside the timed regions.  The plain FP64
+    path is timed on a per-dimension subset for the mixed/plain ratio."""
+    import ctypes as ct
+    import torch
+    from magnus_gb300 import _lib, workloads
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    ds, Ss, ns, seeds = workloads.config3_instances(seed=3, count=10000)
+    count = args.instances or len(ds)
+    order = np.arange(count)
+    wave_bytes = 48 << 30
+    total_ms, total_units = 0.0, 0
+    per_d = {}
+
+    def make_inst(i, prec):
+        d, S, n = int(ds[i]), int(Ss[i]), int(ns[i])
+        C, w = workloads.config0_coeffs(int(seeds[i]), d)
+        t = torch.linspace(0.0, 1.0, S, dtype=torch.float64, device=dev)[:, None, None]
+        Ct = torch.as_tensor(C, device=dev)
+        A = (Ct[0] + Ct[1] * torch.sin(w[0] * t) + Ct[2] * torch.cos(w[1] * t)).to(torch.float32)
+        cot = torch.ones((d, d), dtype=torch.float32, device=dev)
+        prob = _lib.make_problem(kind=0, dtype_code=_lib.DTYPE_F32, precision=prec, op=_lib.OP_SUM, integrator=0,
+                                 n=n, samples=S, dim=d, t0=0.0, tf=1.0)
+        return A, cot, prob
+
+    def run_wave(idx, prec, steps):
+        As, cots, probs = [], [], []
+        for i in idx:
+            A, cot, p = make_inst(i, prec)
+            As.append(A); cots.append(cot); probs.append(p)
+        outs = [torch.empty((a.shape[1], a.shape[1]), dtype=torch.float32, device=dev) for a in As]
+        dAs = [torch.empty_like(a) for a in As]
+        plan = _plan(lib, _lib, probs, As, outs, cots, dAs)
+
+        def step():
+            s = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+            _lib.check(lib.mgb_plan_forward(plan, s))
+            _lib.check(lib.mgb_plan_vjp(plan, s))
+
+        ms = _time_graph(torch, step, steps, warmup=1)
+        lib.mgb_plan_destroy(plan)
+        del As, dAs, outs
+        torch.cuda.empty_cache()
+        return ms
+
+    wave, wbytes = [], 0
+    for i in order:
+        b = int(Ss[i]) * int(ds[i]) ** 2 * 4 * 2
+        if wave and wbytes + b > wave_bytes:
+            total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1)
+            wave, wbytes = [], 0
+        wave.append(int(i))
+        wbytes += b
+        total_units += int(Ss[i]) * int(ns[i])
+    if wave:
+        total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1)
+    # per-dimension mixed vs plain on the same small subsets
+    plain_est_s = 0.0
+    for d in (2, 4, 8, 16, 32, 64, 128):
+        cand = np.nonzero(ds[:count] == d)[0]
+        if len(cand) == 0:
+            continue
+        sel = [int(i) for i in cand[np.argsort(Ss[cand], kind="stable")][:8]]  # shortest of this d
+        units = sum(int(Ss[i]) * int(ns[i]) for i in sel)
+        mixed_ms = run_wave(sel, _lib.PRECISION_MIXED, 1)
+        plain_ms = run_wave(sel, _lib.PRECISION_PLAIN, 1)
+        per_d[d] = {"mixed": units / (mixed_ms / 1e3), "plain_fp64": units / (plain_ms / 1e3),
+                    "ratio": plain_ms / mixed_ms, "instances": len(sel)}
+        # plain FP64 time of all instances of this d, at the subset's rate per unit of work
+        work_d = sum(int(Ss[i]) * (int(ns[i]) - 1) * d ** 3 for i in cand)
+        work_sel = sum(int(Ss[i]) * (int(ns[i]) - 1) * d ** 3 for i in sel)
+        plain_est_s += plain_ms / 1e3 * work_d / max(work_sel, 1)
+    value = total_units / (total_ms / 1e3)
+    print(json.dumps({"workload": f"config3 uneven batch, {count} instances, fwd+VJP, float32",
+                      "metric": "samples·order/s fwd+VJP", "value": value, "ms": total_ms, "precision": "mixed",
+                      "plain_fp64_estimated": {"value": total_units / plain_est_s,
+                                               "how": "per-dimension subset rates scaled by each dimension's (n-1)*S*d^3 work"},
+                      "mixed_over_plain": plain_est_s / (total_ms / 1e3), "per_dimension_subsets": per_d}))
+
+
 # ---------------------------------------------------------------- GPU legs
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "config4":
+        {"config1": run_config1, "config2": run_config2, "config3": run_config3}[args.workload](args)
         return
 
     import torch
