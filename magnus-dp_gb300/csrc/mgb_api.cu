@@ -117,8 +117,12 @@ int rule_divisibility(int integrator) {
     }
 }
 
+// Checkpoint interval.  The mixed form's chunk scans are FP64 (n(n-1)/2
+// products per chunk against (n-1)K FP32 products inside it), so it takes
+// long chunks at every d; the plain form keeps shorter ones at large d,
+// where its slots are twice as large and its scans cost little.
 int default_K(const mgb_problem& p) {
-    if (p.kind == MGB_KIND_SPACECURVE || p.dim <= 32) return 256;
+    if (p.kind == MGB_KIND_SPACECURVE || p.dim <= 32 || p.precision == MGB_PRECISION_MIXED) return 256;
     if (p.dim <= 64) return 128;
     return 64;
 }
@@ -235,6 +239,11 @@ struct Segment {
     int64_t slot_elems = 0, grid = 0;
     size_t scr_off = 0;
     std::vector<InstDev> hi;
+    // chunk scans spread over the GPU (matrix, d a multiple of 16):
+    // active[c] = instances of the segment with more than c chunks
+    bool tiled_scan = false;
+    int d = 0, nmax = 0;
+    std::vector<int32_t> active;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -300,10 +309,13 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     pc.sms = device_info().sms;
     const size_t tsz = pc.plain ? sizeof(double) : sizeof(float);
 
-    // sort by dimension (largest first: heavy segments start first)
+    // sort by dimension (largest first: heavy segments start first), then by
+    // chunk count (the tiled scans launch each step over a prefix)
     pc.order.resize(call.count);
     for (size_t i = 0; i < call.count; ++i) pc.order[i] = (int32_t)i;
-    std::stable_sort(pc.order.begin(), pc.order.end(), [&](int32_t a, int32_t b) { return dv[a].m > dv[b].m; });
+    std::stable_sort(pc.order.begin(), pc.order.end(), [&](int32_t a, int32_t b) {
+        return dv[a].m != dv[b].m ? dv[a].m > dv[b].m : dv[a].C > dv[b].C;
+    });
 
     size_t nwork = 0, gl_doubles = 0, ck_doubles = 0, wsd = 0;
     pc.all_ck_in = call.ckpt_in != nullptr;
@@ -321,7 +333,7 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     // segments: runs of equal dimension
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    const size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 4, (size_t)16 << 30));
+    const size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 2, (size_t)48 << 30));
     int64_t wpos = 0;
     for (size_t a = 0; a < call.count;) {
         size_t b = a;
@@ -343,6 +355,14 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
             I.n = (int32_t)p.n;
             I.K = dv[i].K;
             sg.hi.push_back(I);
+            sg.nmax = std::max<int>(sg.nmax, (int)p.n);
+        }
+        sg.d = sg.hi[0].d;
+        sg.tiled_scan = scan_tiled_ok(pc.kind, sg.d);
+        if (sg.tiled_scan) {
+            sg.active.assign((size_t)dv[pc.order[a]].C, 0);
+            for (size_t k = a; k < b; ++k)
+                for (int c = 0; c < dv[pc.order[k]].C; ++c) ++sg.active[(size_t)c];
         }
         wpos += sg.nwork;
         pc.segs.push_back(std::move(sg));
@@ -355,14 +375,23 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     pc.off_gl = off; off = align_up(off + gl_doubles * sizeof(double), 256);
     pc.off_ck = off; off = align_up(off + ck_doubles * sizeof(double), 256);
     pc.off_ws = off; off = align_up(off + wsd * sizeof(double), 256);
-    for (Segment& sg : pc.segs) {
-        const double share = (double)sg.nwork / (double)std::max<size_t>(nwork, 1);
-        const size_t seg_budget = std::max<size_t>((size_t)64 << 20, (size_t)(budget * share));
-        const SegSizing sz = size_segment(pc.plain, pc.kind, pc.rule, pc.f64io != 0, sg.hi, sg.nwork, pc.sms, seg_budget);
-        sg.slot_elems = sz.slot_elems;
-        sg.grid = sz.grid;
+    // every segment asks for one slot per resident CTA; when the asks exceed
+    // the budget, all are cut in the same proportion
+    std::vector<SegSizing> want(pc.segs.size());
+    double asked = 0.0;
+    for (size_t s = 0; s < pc.segs.size(); ++s) {
+        const Segment& sg = pc.segs[s];
+        want[s] = size_segment(pc.plain, pc.kind, pc.rule, pc.f64io != 0, sg.hi, sg.nwork, pc.sms,
+                               std::numeric_limits<size_t>::max());
+        asked += (double)want[s].grid * (double)want[s].slot_elems * (double)tsz;
+    }
+    const double cut = asked > (double)budget ? (double)budget / asked : 1.0;
+    for (size_t s = 0; s < pc.segs.size(); ++s) {
+        Segment& sg = pc.segs[s];
+        sg.slot_elems = want[s].slot_elems;
+        sg.grid = std::max<int64_t>(1, (int64_t)((double)want[s].grid * cut));
         sg.scr_off = off;
-        off = align_up(off + (size_t)sz.grid * (size_t)sz.slot_elems * tsz, 256);
+        off = align_up(off + (size_t)sg.grid * (size_t)sg.slot_elems * tsz, 256);
     }
     if (pc.any_carry) {
         // the carry record runs the generic kernel over all instances
@@ -488,33 +517,57 @@ LaunchArgs seg_args(const PlanCore& pc, const Segment& sg, cudaStream_t st) {
     return la;
 }
 
-// Chunk kernel of every segment, concurrently when there are several.
-mgb_status plan_chunks(PlanCore& pc, int mode, cudaStream_t st, const char* name) {
-    if (pc.segs.size() == 1) {
-        Segment& sg = pc.segs[0];
-        const LaunchArgs la = seg_args(pc, sg, st);
-        MGB_CUDA_TRY(timed(name, st, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
-        return MGB_OK;
-    }
+// Run f(segment, stream) for every segment: on `st` when there is one, else
+// each on its own stream, forked from and joined back into `st`.
+template <class F>
+mgb_status for_segments(PlanCore& pc, cudaStream_t st, F&& f) {
+    if (pc.segs.size() == 1) return f(pc.segs[0], st);
     MGB_CUDA_TRY(cudaEventRecord(pc.fork, st));
     for (Segment& sg : pc.segs) {
         MGB_CUDA_TRY(cudaStreamWaitEvent(sg.stream, pc.fork, 0));
-        const LaunchArgs la = seg_args(pc, sg, sg.stream);
-        MGB_CUDA_TRY(timed(name, sg.stream, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
+        mgb_status s = f(sg, sg.stream);
+        if (s != MGB_OK) return s;
         MGB_CUDA_TRY(cudaEventRecord(sg.done, sg.stream));
     }
     for (Segment& sg : pc.segs) MGB_CUDA_TRY(cudaStreamWaitEvent(st, sg.done, 0));
     return MGB_OK;
 }
 
+mgb_status seg_chunks(PlanCore& pc, Segment& sg, int mode, cudaStream_t s, const char* name) {
+    const LaunchArgs la = seg_args(pc, sg, s);
+    MGB_CUDA_TRY(timed(name, s, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
+    return MGB_OK;
+}
+
+// Forward scan over a segment's chunks: pi^0..pi^C.
+mgb_status seg_scan(PlanCore& pc, Segment& sg, cudaStream_t s) {
+    const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
+    if (sg.tiled_scan)
+        MGB_CUDA_TRY(timed("scan", s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, false, pc.f64io, s); }));
+    else
+        MGB_CUDA_TRY(timed("scan", s, [&] { return launch_small(true, pc.kind, SMALL_SCAN, di, sg.count, pc.f64io, 0, s); }));
+    return MGB_OK;
+}
+
+mgb_status seg_small(PlanCore& pc, Segment& sg, int which, int write_out, cudaStream_t s, const char* name) {
+    const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
+    if (which == SMALL_RSCAN && sg.tiled_scan)
+        MGB_CUDA_TRY(timed(name, s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, true, pc.f64io, s); }));
+    else
+        MGB_CUDA_TRY(timed(name, s, [&] { return launch_small(true, pc.kind, which, di, sg.count, pc.f64io, write_out, s); }));
+    return MGB_OK;
+}
+
 mgb_status plan_forward(PlanCore& pc, cudaStream_t st) {
     if (!pc.has_out) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
     const InstDev* d_inst = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst);
-    const int cnt = (int)pc.count;
-    mgb_status s = plan_chunks(pc, MODE_LOCAL, st, "chunk_local");
+    mgb_status s = for_segments(pc, st, [&](Segment& sg, cudaStream_t ss) {
+        mgb_status r = seg_chunks(pc, sg, MODE_LOCAL, ss, "chunk_local");
+        if (r == MGB_OK) r = seg_scan(pc, sg, ss);
+        if (r == MGB_OK) r = seg_small(pc, sg, SMALL_FIN_FWD, 1, ss, "fin_fwd");
+        return r;
+    });
     if (s != MGB_OK) return s;
-    MGB_CUDA_TRY(timed("scan", st, [&] { return launch_small(true, pc.kind, SMALL_SCAN, d_inst, cnt, pc.f64io, 0, st); }));
-    MGB_CUDA_TRY(timed("fin_fwd", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_FWD, d_inst, cnt, pc.f64io, 1, st); }));
     if (pc.any_carry) {
         LaunchArgs la;
         la.insts = d_inst;
@@ -532,17 +585,18 @@ mgb_status plan_forward(PlanCore& pc, cudaStream_t st) {
 
 mgb_status plan_vjp(PlanCore& pc, cudaStream_t st, bool recompute) {
     if (!pc.has_vjp) return fail(MGB_ERR_INVALID_ARGUMENT, "cotangent and dA buffers were not given to this plan");
-    const InstDev* d_inst = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst);
-    const int cnt = (int)pc.count;
-    if (recompute) {
-        mgb_status s = plan_chunks(pc, MODE_LOCAL, st, "chunk_local");
-        if (s != MGB_OK) return s;
-        MGB_CUDA_TRY(timed("scan", st, [&] { return launch_small(true, pc.kind, SMALL_SCAN, d_inst, cnt, pc.f64io, 0, st); }));
-    }
-    MGB_CUDA_TRY(timed("fin_fwd", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_FWD, d_inst, cnt, pc.f64io, 0, st); }));
-    MGB_CUDA_TRY(timed("fin_vjp", st, [&] { return launch_small(true, pc.kind, SMALL_FIN_VJP, d_inst, cnt, pc.f64io, 0, st); }));
-    MGB_CUDA_TRY(timed("rscan", st, [&] { return launch_small(true, pc.kind, SMALL_RSCAN, d_inst, cnt, pc.f64io, 0, st); }));
-    return plan_chunks(pc, MODE_VJP, st, "chunk_vjp");
+    return for_segments(pc, st, [&](Segment& sg, cudaStream_t ss) {
+        mgb_status r = MGB_OK;
+        if (recompute) {
+            r = seg_chunks(pc, sg, MODE_LOCAL, ss, "chunk_local");
+            if (r == MGB_OK) r = seg_scan(pc, sg, ss);
+        }
+        if (r == MGB_OK) r = seg_small(pc, sg, SMALL_FIN_FWD, 0, ss, "fin_fwd");
+        if (r == MGB_OK) r = seg_small(pc, sg, SMALL_FIN_VJP, 0, ss, "fin_vjp");
+        if (r == MGB_OK) r = seg_small(pc, sg, SMALL_RSCAN, 0, ss, "rscan");
+        if (r == MGB_OK) r = seg_chunks(pc, sg, MODE_VJP, ss, "chunk_vjp");
+        return r;
+    });
 }
 
 // One-shot call: plan in stream-ordered memory, run, release.

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "mgb_common.cuh"
@@ -29,5 +30,14 @@ cudaError_t launch_generic_chunk(bool fp64, int kind, int rule, int mode, const 
 // Per-instance small math, one CTA per instance.
 cudaError_t launch_small(bool fp64, int kind, int which, const InstDev* insts, int count, int f64io, int write_out,
                          cudaStream_t st);
+
+// Chunk scans spread over the GPU (mgb_scan.cu), for matrix instances with
+// d a multiple of 16.  `insts` are `count` instances of one dimension sorted
+// by chunk count (descending); active[c] = number of them with C > c.  The
+// forward pass writes pi^0..pi^C; the reverse pass rho^{C-1}..rho^0 (from
+// tau) and zeroes the dA rows shared by two chunks.
+bool scan_tiled_ok(int kind, int d);
+cudaError_t launch_scan_tiled(const InstDev* insts, int count, int d, int nmax, const std::vector<int32_t>& active,
+                              bool reverse, int f64io, cudaStream_t st);
 
 }  // namespace mgb

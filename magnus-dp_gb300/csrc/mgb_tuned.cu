@@ -503,6 +503,9 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
     if (tc.use && tc.family == 1) {
         sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4;  // one thread's tape
         want = std::min<int64_t>(nwork, (int64_t)sms * 1024);
+    } else if (tc.use) {
+        sz.slot_elems = generic;
+        want = std::min<int64_t>(nwork, (int64_t)sms * tc.ctas_per_sm);
     } else {
         sz.slot_elems = generic;
         want = std::min<int64_t>(nwork, (int64_t)sms * 8);
