@@ -146,6 +146,13 @@ mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, void* out, v
 mgb_status mgb_set_gl_table(size_t max_order, const double* weights, const double* nodes);
 size_t mgb_max_order(void);
 
+/* Engine-specific, no reference counterpart.  Synchronizes the current
+ * device and returns MGB_ERR_DEVICE_TIMEOUT if a kernel gave up one of its
+ * bounded device-side waits since the last check (its outputs are then
+ * invalid).  The host entry points check this themselves; callers of the
+ * device entry points and plans check it when they synchronize. */
+mgb_status mgb_device_check(void);
+
 /* Kernel timing.  While enabled, every engine kernel launch is bracketed by
  * CUDA events on its stream; mgb_profile_read waits for the recorded events,
  * fills up to `capacity` entries (one per kernel name: launches and total

@@ -818,6 +818,7 @@ mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void
         e = cudaMemcpy(out, dO, no * es, cudaMemcpyDeviceToHost);
         if (e == cudaSuccess && dC) e = cudaMemcpy(carry, dC, nc * es, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) st = fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+        else if (read_clear_device_timeout()) st = fail(MGB_ERR_DEVICE_TIMEOUT, "a device-side wait timed out");
     }
     cleanup();
     return st;
@@ -853,6 +854,7 @@ mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, vo
     if (st == MGB_OK) {
         e = cudaMemcpy(dA, dOut, ni * es, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) st = fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+        else if (read_clear_device_timeout()) st = fail(MGB_ERR_DEVICE_TIMEOUT, "a device-side wait timed out");
     }
     cleanup();
     return st;
@@ -874,6 +876,14 @@ mgb_status mgb_set_gl_table(size_t max_order, const double* weights, const doubl
 }
 
 size_t mgb_max_order(void) { return gl_snapshot()->max_order; }
+
+mgb_status mgb_device_check(void) {
+    g_last_error.clear();
+    const cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(MGB_ERR_CUDA, cudaGetErrorString(e));
+    if (read_clear_device_timeout()) return fail(MGB_ERR_DEVICE_TIMEOUT, "a device-side wait timed out");
+    return MGB_OK;
+}
 
 const char* mgb_last_error(void) { return g_last_error.c_str(); }
 

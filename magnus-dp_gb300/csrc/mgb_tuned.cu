@@ -452,8 +452,10 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     if (plain || f64io || kind != KIND_MATRIX) return tc;
     const int D = hi[0].d;
     if (D == 64 || D == 128) {
-        for (const InstDev& I : hi)
+        for (const InstDev& I : hi) {
             if (I.d != D || reinterpret_cast<uintptr_t>(I.A) % 16 != 0) return tc;
+            if (mode == MODE_VJP && reinterpret_cast<uintptr_t>(I.dA) % 16 != 0) return tc;
+        }
         tc.use = true;
         tc.family = 3;
         tc.D = D;

@@ -28,7 +28,11 @@ cudaError_t launch_small_family(bool plain, int kind, int rule, int mode, const 
 int small_family_max_levels();
 
 TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi);
-cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, bool prepare_only);
+// Tensor-core chunk kernel (mgb_bigtc.cu) for the mixed form at d = 64 / 128;
+// `ctas` caps the grid.
+cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int ctas, bool prepare_only);
+// 1 if a kernel gave up a bounded device-side wait since the last call.
+int read_clear_device_timeout();
 cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode);
 cudaError_t launch_tuned(const TunedChoice& tc, bool plain, int kind, int rule, int mode, const LaunchArgs& a, int sms);
 cudaError_t launch_chunk_any(bool plain, int kind, int rule, int mode, const LaunchArgs& a,
