@@ -151,63 +151,59 @@ __device__ __forceinline__ uint32_t core_off(int row, int kc) {
     return (uint32_t)kc * TcCfg<D>::LBO + (uint32_t)(row >> 3) * TcCfg<D>::SBO + (uint32_t)(row & 7) * 16;
 }
 
-// Tile (row, k) for k in block kb: TRANS ? src[k][row] : src[row][k]
-// (src row-major D x D in global memory), split into the three pieces at
-// t, t + TILE, t + 2 TILE.  Plain loads: the chunk buffers are written by
-// this kernel.
+// One k-block of an operand tile, element (row, k) = TRANS ? src[k][row] :
+// src[row][k] (src row-major D x D in global memory), held in registers
+// between its load and its store to shared memory so that the loads of the
+// next block overlap the MMAs and the epilogue.  Item = (row, 8 consecutive
+// k): direct loads are one 32-byte sector per thread, transposed loads eight
+// 4-byte loads coalesced across the warp; the stores are one 16-byte chunk
+// per piece, consecutive rows at consecutive 16 bytes (no bank conflicts).
+// Plain loads: the chunk buffers are written by this kernel.
+template <int D>
+struct TileRegs {
+    static constexpr int NI = D * (KB / 8) / TNT;  // items per thread
+    float v[NI][8];
+};
+
 template <int D, bool TRANS>
-__device__ __forceinline__ void stage_tile(uint8_t* t, const float* __restrict__ src, int kb) {
-    constexpr uint32_t TL = TcCfg<D>::TILE;
-    const int tid = threadIdx.x;
-    if (!TRANS) {
-        // item = (row, 8 consecutive k): one 32-byte sector, one chunk per piece
-        for (int it = tid; it < D * (KB / 8); it += TNT) {
-            const int row = it % D, s8 = it / D;
+__device__ __forceinline__ void load_tile(TileRegs<D>& r, const float* __restrict__ src, int kb) {
+#pragma unroll
+    for (int i = 0; i < TileRegs<D>::NI; ++i) {
+        const int it = threadIdx.x + i * TNT, row = it % D, s8 = it / D;
+        if (!TRANS) {
             const float* p = src + (int64_t)row * D + kb * KB + s8 * 8;
             const float4 a = *reinterpret_cast<const float4*>(p);
             const float4 b = *reinterpret_cast<const float4*>(p + 4);
-            const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-            uint32_t w[3][4];
+            r.v[i][0] = a.x; r.v[i][1] = a.y; r.v[i][2] = a.z; r.v[i][3] = a.w;
+            r.v[i][4] = b.x; r.v[i][5] = b.y; r.v[i][6] = b.z; r.v[i][7] = b.w;
+        } else {
+            const float* p = src + (int64_t)(kb * KB + s8 * 8) * D + row;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                uint16_t l0, l1, l2, h0, h1, h2;
-                split3(v[2 * i], l0, l1, l2);
-                split3(v[2 * i + 1], h0, h1, h2);
-                w[0][i] = (uint32_t)l0 | ((uint32_t)h0 << 16);
-                w[1][i] = (uint32_t)l1 | ((uint32_t)h1 << 16);
-                w[2][i] = (uint32_t)l2 | ((uint32_t)h2 << 16);
-            }
-            const uint32_t o = core_off<D>(row, s8);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4*>(t + q * TL + o) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+            for (int u = 0; u < 8; ++u) r.v[i][u] = p[(int64_t)u * D];
         }
-    } else {
-        // item = (4 rows, 4 k): four float4 loads along rows, transposed;
-        // half a chunk (8 bytes) per row and piece
-        for (int it = tid; it < (D / 4) * (KB / 4); it += TNT) {
-            const int rq = it % (D / 4), kq = it / (D / 4);
-            const float* p = src + (int64_t)(kb * KB + kq * 4) * D + rq * 4;
-            float4 v[4];
+    }
+}
+
+// Split the held block into three BF16 pieces at t, t + TILE, t + 2 TILE.
+template <int D>
+__device__ __forceinline__ void store_tile(uint8_t* t, const TileRegs<D>& r) {
+    constexpr uint32_t TL = TcCfg<D>::TILE;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = *reinterpret_cast<const float4*>(p + (int64_t)u * D);
-            const float c[4][4] = {{v[0].x, v[1].x, v[2].x, v[3].x},
-                                   {v[0].y, v[1].y, v[2].y, v[3].y},
-                                   {v[0].z, v[1].z, v[2].z, v[3].z},
-                                   {v[0].w, v[1].w, v[2].w, v[3].w}};
+    for (int i = 0; i < TileRegs<D>::NI; ++i) {
+        const int it = threadIdx.x + i * TNT, row = it % D, s8 = it / D;
+        uint32_t w[3][4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                uint16_t q0[4], q1[4], q2[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) split3(c[j][u], q0[u], q1[u], q2[u]);
-                const uint32_t o = core_off<D>(rq * 4 + j, kq >> 1) + (uint32_t)(kq & 1) * 8;
-                *reinterpret_cast<uint2*>(t + o) =
-                    make_uint2((uint32_t)q0[0] | ((uint32_t)q0[1] << 16), (uint32_t)q0[2] | ((uint32_t)q0[3] << 16));
-                *reinterpret_cast<uint2*>(t + TL + o) =
-                    make_uint2((uint32_t)q1[0] | ((uint32_t)q1[1] << 16), (uint32_t)q1[2] | ((uint32_t)q1[3] << 16));
-                *reinterpret_cast<uint2*>(t + 2 * TL + o) =
-                    make_uint2((uint32_t)q2[0] | ((uint32_t)q2[1] << 16), (uint32_t)q2[2] | ((uint32_t)q2[3] << 16));
-            }
+        for (int h = 0; h < 4; ++h) {
+            uint16_t l0, l1, l2, h0, h1, h2;
+            split3(r.v[i][2 * h], l0, l1, l2);
+            split3(r.v[i][2 * h + 1], h0, h1, h2);
+            w[0][h] = (uint32_t)l0 | ((uint32_t)h0 << 16);
+            w[1][h] = (uint32_t)l1 | ((uint32_t)h1 << 16);
+            w[2][h] = (uint32_t)l2 | ((uint32_t)h2 << 16);
         }
+        const uint32_t o = core_off<D>(row, s8);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) *reinterpret_cast<uint4*>(t + q * TL + o) = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
     }
 }
 
@@ -268,6 +264,9 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
     constexpr int m = Cf::m;
     const int cnt = l1 - l0 + 1;
     if (cnt <= 0) return true;
+    TileRegs<D> rx, ry;
+    load_tile<D, XT>(rx, X + (int64_t)l0 * m, 0);
+    load_tile<D, YT>(ry, Y + (int64_t)l0 * m, 0);
     for (int idx = 0; idx <= cnt; ++idx) {
         if (idx < cnt) {
             const int li = l0 + idx;
@@ -278,8 +277,8 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
                 uint8_t* xs = pp.stg + (size_t)b * Cf::STAGE;
                 uint8_t* ys = xs + 3 * Cf::TILE;
                 if (pp.ok) {
-                    stage_tile<D, XT>(xs, X + (int64_t)li * m, kb);
-                    stage_tile<D, YT>(ys, Y + (int64_t)li * m, kb);
+                    store_tile<D>(xs, rx);
+                    store_tile<D>(ys, ry);
                 }
                 fence_async_smem();
                 if (__syncthreads_or(!pp.ok)) return false;
@@ -308,6 +307,13 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
                     if (kb == Cf::NKB - 1) mma_commit(pp.mb + 8 * (2 + a));
                 }
                 ++pp.kt;
+                // operands of the next k-block (this sample's or the next one's)
+                const int nkb = kb + 1 < Cf::NKB ? kb + 1 : 0;
+                const int nli = kb + 1 < Cf::NKB ? li : li + 1;
+                if (nli <= l1) {
+                    load_tile<D, XT>(rx, X + (int64_t)nli * m, nkb);
+                    load_tile<D, YT>(ry, Y + (int64_t)nli * m, nkb);
+                }
                 if (kb == 0 && idx > 0) epilogue<D>(pp, pp.ns - 1, out + (int64_t)(li - 1) * m, add);
             }
             ++pp.ns;
