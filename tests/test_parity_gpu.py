@@ -242,8 +242,9 @@ def test_tiled_kernel_orders(n, cuda):
 @pytest.mark.parametrize("integrator,S", [("Boole", 129), ("Simpson", 131), ("Trapezoid", 97), ("Riemann", 90)])
 @pytest.mark.parametrize("d", [64, 128])
 def test_big_mixed_kernel_float32(integrator, S, d, cuda):
-    """float32 inputs at d = 64 / 128 in mixed precision run the level-major
-    shared-memory tiled kernel (mgb_big.cu); orders and VJP within 1e-6."""
+    """float32 inputs at d = 64 / 128 in mixed precision run the tensor-core
+    chunk kernel (mgb_bigtc.cu, tcgen05 on BF16 operand pieces); orders and
+    VJP within 1e-6."""
     A = smooth_samples(S, d, seed=d + 5).astype(np.float32)
     A64 = A.astype(np.float64)
     n = 4
