@@ -164,61 +164,72 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
         __syncthreads();
 
         // ---------------- forward over the groups ----------------
+        // Global loads run one step ahead of their use: the next group's A
+        // during this group's levels, the next level's prefix state (and
+        // carry) during this level's product.
+        constexpr int NV = G * m / 4 / TNT;  // float4 per thread per group
+        float4 va[NV];
+        // A is read-only for the launch (non-coherent path); the tape is
+        // written by this kernel (plain loads)
+        auto load_group = [&](float4 (&v)[NV], const float* src, int nvalid, bool ro) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) {
+                const int i4 = tid + q * TNT;
+                const float4* p = reinterpret_cast<const float4*>(src) + i4;
+                v[q] = (i4 * 4 < nvalid) ? (ro ? __ldg(p) : *p) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        };
+        FwdState<float> fs[EPT];
+        double fpv[EPT];
+        auto load_fstate = [&](int j) {
+            const float* sj = st + (j - 1) * 3 * m;
+#pragma unroll
+            for (int q = 0; q < EPT; ++q) {
+                const int el = tid + q * TNT;
+                fs[q].base = sj[el];
+                fs[q].blo = sj[m + el];
+                fs[q].f0 = sj[2 * m + el];
+                fs[q].f1 = fs[q].f2 = fs[q].f3 = 0.f;
+                fpv[q] = (MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el];
+            }
+        };
+        load_group(va, Ag + (int64_t)first * m, min(G, Kp - first + 1) * m, true);
         for (int li0 = first; li0 <= Kp; li0 += G) {
             const int ge = min(G, Kp - li0 + 1);
-            {
-                constexpr int NV = G * m / 4 / TNT;  // float4 per thread
-                const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
-                float4 v[NV];
 #pragma unroll
-                for (int q = 0; q < NV; ++q) {
-                    const int i4 = tid + q * TNT;
-                    v[q] = (i4 * 4 < ge * m) ? __ldg(src + i4) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-#pragma unroll
-                for (int q = 0; q < NV; ++q) {
-                    const int i4 = tid + q * TNT;
-                    const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                    *reinterpret_cast<float4*>(sF + l * D * P4 + r * P4 + cc) = v[q];
-                    float* at = sAT + l * D * P4 + r;
-                    at[(cc + 0) * P4] = v[q].x;
-                    at[(cc + 1) * P4] = v[q].y;
-                    at[(cc + 2) * P4] = v[q].z;
-                    at[(cc + 3) * P4] = v[q].w;
-                }
+            for (int q = 0; q < NV; ++q) {
+                const int i4 = tid + q * TNT;
+                const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                *reinterpret_cast<float4*>(sF + l * D * P4 + r * P4 + cc) = va[q];
+                float* at = sAT + l * D * P4 + r;
+                at[(cc + 0) * P4] = va[q].x;
+                at[(cc + 1) * P4] = va[q].y;
+                at[(cc + 2) * P4] = va[q].z;
+                at[(cc + 3) * P4] = va[q].w;
             }
+            if (li0 + G <= Kp) load_group(va, Ag + (int64_t)(li0 + G) * m, min(G, Kp - li0 - G + 1) * m, true);
+            load_fstate(1);
             __syncthreads();
             for (int j = 1; j <= NLf; ++j) {
                 {
                     float* sj = st + (j - 1) * 3 * m;
-                    FwdState<float> s[EPT];
-                    double pv[EPT];
-#pragma unroll
-                    for (int q = 0; q < EPT; ++q) {  // all global loads first
-                        const int el = tid + q * TNT;
-                        s[q].base = sj[el];
-                        s[q].blo = sj[m + el];
-                        s[q].f0 = sj[2 * m + el];
-                        s[q].f1 = s[q].f2 = s[q].f3 = 0.f;
-                        pv[q] = (MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el];
-                    }
 #pragma unroll
                     for (int q = 0; q < EPT; ++q) {
                         const int el = tid + q * TNT, r = el / D, cc = el % D;
-                        const Carry<float> cy = split_carry<float>(pv[q]);
+                        const Carry<float> cy = split_carry<float>(fpv[q]);
                         for (int l = 0; l < ge; ++l) {
-                            const float P = fwd_step<float, RULE>(s[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
+                            const float P = fwd_step<float, RULE>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
                             sP[l * D * P4 + r * P4 + cc] = P;
-                            // tape rows hold P^T so the adjoint reloads them contiguously
-                            if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + cc * D + r] = P;
+                            if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
                         }
-                        sj[el] = s[q].base;
-                        sj[m + el] = s[q].blo;
-                        sj[2 * m + el] = s[q].f0;
+                        sj[el] = fs[q].base;
+                        sj[m + el] = fs[q].blo;
+                        sj[2 * m + el] = fs[q].f0;
                     }
                 }
                 __syncthreads();
                 if (j < NLf) {
+                    load_fstate(j + 1);
                     if (tl < ge) {
                         float acc[4][4] = {};
                         mma_tv<D>(acc, sAT + tl * D * P4, P4, sP + tl * D * P4, P4, r0, c0);
@@ -253,42 +264,51 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                 }
             float* dAg = static_cast<float*>(I.dA) + b * m;
             const int last0 = first + ((Kp - first) / G) * G;
+            // the tape of the next level and that level's reverse state (and
+            // carry) are loaded one level ahead of their use
+            float4 vt[NV];
+            RevState<float> rs[EPT];
+            double rv[EPT];
+            auto load_rstate = [&](int j) {
+                const float* sj = st + (j - 1) * 3 * m;
+#pragma unroll
+                for (int q = 0; q < EPT; ++q) {
+                    const int el = tid + q * TNT;
+                    rs[q].Rb = sj[el];
+                    rs[q].rlo = sj[m + el];
+                    rs[q].pend = sj[2 * m + el];
+                    rs[q].R4l = rs[q].R4 = rs[q].H2 = rs[q].H3 = 0.f;
+                    rv[q] = rc[(int64_t)(j - 1) * m + el];
+                }
+            };
             for (int li0 = last0; li0 >= first; li0 -= G) {
                 const int ge = min(G, Kp - li0 + 1);
-                {
-                    constexpr int NV = G * m / 4 / TNT;
-                    const float4* src = reinterpret_cast<const float4*>(Ag + (int64_t)li0 * m);
-                    float4 v[NV];
+                load_group(va, Ag + (int64_t)li0 * m, ge * m, true);
+                if (n > 1) load_group(vt, tape + ((int64_t)(n - 2) * L + li0) * m, ge * m, false);
+                load_rstate(n);
 #pragma unroll
-                    for (int q = 0; q < NV; ++q) {
-                        const int i4 = tid + q * TNT;
-                        v[q] = (i4 * 4 < ge * m) ? __ldg(src + i4) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-#pragma unroll
-                    for (int q = 0; q < NV; ++q) {
-                        const int i4 = tid + q * TNT;
-                        const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                        *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = v[q];
-                    }
+                for (int q = 0; q < NV; ++q) {
+                    const int i4 = tid + q * TNT;
+                    const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                    *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = va[q];
                 }
                 float dacc[4][4] = {};
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
-                        constexpr int NV = G * m / 4 / TNT;
-                        const float4* src = reinterpret_cast<const float4*>(tape + ((int64_t)(j - 1) * L + li0) * m);
-                        float4 v[NV];
+                        // P_j (row-major on the tape) -> P^T in shared memory
 #pragma unroll
                         for (int q = 0; q < NV; ++q) {
                             const int i4 = tid + q * TNT;
-                            v[q] = (i4 * 4 < ge * m) ? src[i4] : make_float4(0.f, 0.f, 0.f, 0.f);
-                        }
-#pragma unroll
-                        for (int q = 0; q < NV; ++q) {
-                            const int i4 = tid + q * TNT;
-                            const int l = (i4 * 4) / m, el = (i4 * 4) % m, k = el / D, cc = el % D;
-                            *reinterpret_cast<float4*>(sPT + l * D * P4 + k * P4 + cc) = v[q];
+                            const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                            float* pt = sPT + l * D * P4 + r;
+                            pt[(cc + 0) * P4] = vt[q].x;
+                            pt[(cc + 1) * P4] = vt[q].y;
+                            pt[(cc + 2) * P4] = vt[q].z;
+                            pt[(cc + 3) * P4] = vt[q].w;
                         }
                         __syncthreads();
+                        load_rstate(j);
+                        if (j > 1) load_group(vt, tape + ((int64_t)(j - 2) * L + li0) * m, ge * m, false);
                         if (tl < ge) {
                             float hacc[4][4] = {};
                             mma_adjL<D>(hacc, sA + tl * D * P4, sG + tl * D * P1, r0, c0);
@@ -302,28 +322,17 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                     __syncthreads();
                     {
                         float* sj = st + (j - 1) * 3 * m;
-                        RevState<float> s[EPT];
-                        double rv[EPT];
-#pragma unroll
-                        for (int q = 0; q < EPT; ++q) {  // all global loads first
-                            const int el = tid + q * TNT;
-                            s[q].Rb = sj[el];
-                            s[q].rlo = sj[m + el];
-                            s[q].pend = sj[2 * m + el];
-                            s[q].R4l = s[q].R4 = s[q].H2 = s[q].H3 = 0.f;
-                            rv[q] = rc[(int64_t)(j - 1) * m + el];
-                        }
 #pragma unroll
                         for (int q = 0; q < EPT; ++q) {
                             const int el = tid + q * TNT, r = el / D, cc = el % D;
                             const Carry<float> cy = split_carry<float>(rv[q]);
                             for (int l = ge - 1; l >= 0; --l) {
                                 const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
-                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(s[q], H, li0 + l, kc, cy);
+                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, li0 + l, kc, cy);
                             }
-                            sj[el] = s[q].Rb;
-                            sj[m + el] = s[q].rlo;
-                            sj[2 * m + el] = s[q].pend;
+                            sj[el] = rs[q].Rb;
+                            sj[m + el] = rs[q].rlo;
+                            sj[2 * m + el] = rs[q].pend;
                         }
                     }
                     __syncthreads();
