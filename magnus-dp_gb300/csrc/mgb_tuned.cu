@@ -128,9 +128,26 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
         const double* pic = I.pi + (int64_t)c * nm;
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         const int NLf = (MODE == MODE_LOCAL) ? n : n - 1;  // levels with a forward prefix
-        // per-level prefix state [n][3][m] (L2-resident), then the tape [n-1][L][m]
+        // per-level prefix state [n][3][m] (L2-resident), the tape [n-1][L][m],
+        // then (VJP) the chunk carries pi^c and rho^c split into FP32 hi / lo
+        // once per chunk, [2][n][2][m] (FP64 conversions cost a 1/64-rate pipe)
         float* const st = slot;
         float* const tape = slot + (int64_t)3 * n * m;
+        float* const cyt = tape + (int64_t)(n - 1) * L * m;
+        if (MODE == MODE_VJP) {
+            const double* rcc = I.rho + (int64_t)c * nm;
+            for (int j = 1; j <= n; ++j)
+#pragma unroll
+                for (int q = 0; q < EPT; ++q) {
+                    const int el = tid + q * TNT;
+                    const Carry<float> a = split_carry<float>(riem0 ? 0.0 : pic[(int64_t)(j - 1) * m + el]);
+                    const Carry<float> r = split_carry<float>(rcc[(int64_t)(j - 1) * m + el]);
+                    cyt[((int64_t)(j - 1) * 2) * m + el] = a.hi;
+                    cyt[((int64_t)(j - 1) * 2 + 1) * m + el] = a.lo;
+                    cyt[((int64_t)(n + j - 1) * 2) * m + el] = r.hi;
+                    cyt[((int64_t)(n + j - 1) * 2 + 1) * m + el] = r.lo;
+                }
+        }
 
         // ---------------- forward state at the chunk start ----------------
         for (int j = 1; j <= NLf; ++j)
@@ -180,7 +197,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             }
         };
         FwdState<float> fs[EPT];
-        double fpv[EPT];
+        Carry<float> fcy[EPT];
         auto load_fstate = [&](int j) {
             const float* sj = st + (j - 1) * 3 * m;
 #pragma unroll
@@ -190,7 +207,12 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                 fs[q].blo = sj[m + el];
                 fs[q].f0 = sj[2 * m + el];
                 fs[q].f1 = fs[q].f2 = fs[q].f3 = 0.f;
-                fpv[q] = (MODE == MODE_LOCAL || riem0) ? 0.0 : pic[(int64_t)(j - 1) * m + el];
+                if (MODE == MODE_LOCAL) {
+                    fcy[q].hi = fcy[q].lo = 0.f;
+                } else {
+                    fcy[q].hi = cyt[((int64_t)(j - 1) * 2) * m + el];
+                    fcy[q].lo = cyt[((int64_t)(j - 1) * 2 + 1) * m + el];
+                }
             }
         };
         load_group(va, Ag + (int64_t)first * m, min(G, Kp - first + 1) * m, true);
@@ -216,7 +238,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
 #pragma unroll
                     for (int q = 0; q < EPT; ++q) {
                         const int el = tid + q * TNT, r = el / D, cc = el % D;
-                        const Carry<float> cy = split_carry<float>(fpv[q]);
+                        const Carry<float> cy = fcy[q];
                         for (int l = 0; l < ge; ++l) {
                             const float P = fwd_step<float, RULE>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
                             sP[l * D * P4 + r * P4 + cc] = P;
@@ -254,7 +276,6 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
 
         if (MODE == MODE_VJP) {
             __syncthreads();
-            const double* rc = I.rho + (int64_t)c * nm;
             for (int j = 1; j <= n; ++j)
                 for (int q = 0; q < EPT; ++q) {
                     const int el = tid + q * TNT;
@@ -268,7 +289,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             // carry) are loaded one level ahead of their use
             float4 vt[NV];
             RevState<float> rs[EPT];
-            double rv[EPT];
+            Carry<float> rcy[EPT];
             auto load_rstate = [&](int j) {
                 const float* sj = st + (j - 1) * 3 * m;
 #pragma unroll
@@ -278,7 +299,8 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                     rs[q].rlo = sj[m + el];
                     rs[q].pend = sj[2 * m + el];
                     rs[q].R4l = rs[q].R4 = rs[q].H2 = rs[q].H3 = 0.f;
-                    rv[q] = rc[(int64_t)(j - 1) * m + el];
+                    rcy[q].hi = cyt[((int64_t)(n + j - 1) * 2) * m + el];
+                    rcy[q].lo = cyt[((int64_t)(n + j - 1) * 2 + 1) * m + el];
                 }
             };
             for (int li0 = last0; li0 >= first; li0 -= G) {
@@ -325,7 +347,7 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
 #pragma unroll
                         for (int q = 0; q < EPT; ++q) {
                             const int el = tid + q * TNT, r = el / D, cc = el % D;
-                            const Carry<float> cy = split_carry<float>(rv[q]);
+                            const Carry<float> cy = rcy[q];
                             for (int l = ge - 1; l >= 0; --l) {
                                 const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
                                 sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, li0 + l, kc, cy);
@@ -507,7 +529,7 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
     for (const InstDev& I : hi) {
         const int64_t L = std::min<int64_t>((int64_t)I.K, I.S - 1) + 1;
         Lmax = std::max(Lmax, L);
-        generic = std::max<int64_t>(generic, (int64_t)(I.n + 4) * L * I.m + 3 * (int64_t)I.n * I.m);
+        generic = std::max<int64_t>(generic, (int64_t)(I.n + 4) * L * I.m + 7 * (int64_t)I.n * I.m);
     }
     TunedChoice tc = choose_tuned(plain, kind, rule, MODE_VJP, f64io, hi);
     int64_t want;
