@@ -234,16 +234,21 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
             __syncthreads();
             for (int j = 1; j <= NLf; ++j) {
                 {
+                    // samples outer, the thread's EPT elements inner: EPT
+                    // independent dependency chains interleave
                     float* sj = st + (j - 1) * 3 * m;
+                    for (int l = 0; l < ge; ++l) {
 #pragma unroll
-                    for (int q = 0; q < EPT; ++q) {
-                        const int el = tid + q * TNT, r = el / D, cc = el % D;
-                        const Carry<float> cy = fcy[q];
-                        for (int l = 0; l < ge; ++l) {
-                            const float P = fwd_step<float, RULE>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, cy);
+                        for (int q = 0; q < EPT; ++q) {
+                            const int el = tid + q * TNT, r = el / D, cc = el % D;
+                            const float P = fwd_step<float, RULE>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, fcy[q]);
                             sP[l * D * P4 + r * P4 + cc] = P;
                             if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
                         }
+                    }
+#pragma unroll
+                    for (int q = 0; q < EPT; ++q) {
+                        const int el = tid + q * TNT;
                         sj[el] = fs[q].base;
                         sj[m + el] = fs[q].blo;
                         sj[2 * m + el] = fs[q].f0;
@@ -344,14 +349,17 @@ __global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ ins
                     __syncthreads();
                     {
                         float* sj = st + (j - 1) * 3 * m;
+                        for (int l = ge - 1; l >= 0; --l) {
+#pragma unroll
+                            for (int q = 0; q < EPT; ++q) {
+                                const int el = tid + q * TNT, r = el / D, cc = el % D;
+                                const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
+                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, li0 + l, kc, rcy[q]);
+                            }
+                        }
 #pragma unroll
                         for (int q = 0; q < EPT; ++q) {
-                            const int el = tid + q * TNT, r = el / D, cc = el % D;
-                            const Carry<float> cy = rcy[q];
-                            for (int l = ge - 1; l >= 0; --l) {
-                                const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
-                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, li0 + l, kc, cy);
-                            }
+                            const int el = tid + q * TNT;
                             sj[el] = rs[q].Rb;
                             sj[m + el] = rs[q].rlo;
                             sj[2 * m + el] = rs[q].pend;
