@@ -103,7 +103,11 @@ mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* c
  * buffers (A; out for the forward; cot and dA for the VJP — either pair may
  * be NULL) and prepares everything the engine needs on the device (one
  * cudaMalloc, descriptors uploaded, instances of equal dimension grouped into
- * segments that run concurrently).  mgb_plan_forward / mgb_plan_vjp then only
+ * segments that run concurrently, each segment's chunk-kernel launch variant
+ * picked by timing the variants on a sample of its chunks — once per shape
+ * per process, with a temporary allocation; MGB_AUTOTUNE=0 disables, and
+ * the one-shot entry points do the same when their stream is not being
+ * captured).  mgb_plan_forward / mgb_plan_vjp then only
  * enqueue kernels on `stream`, so they can be captured into a CUDA graph and
  * replayed.  The VJP reuses the checkpoints of the plan's last forward (or
  * recomputes them when the plan has not run forward yet).  Replaces the
@@ -116,6 +120,12 @@ mgb_status mgb_plan_create(const mgb_problem* probs, size_t count, const void* c
 mgb_status mgb_plan_forward(mgb_plan* plan, void* stream);
 mgb_status mgb_plan_vjp(mgb_plan* plan, void* stream);
 size_t mgb_plan_bytes(const mgb_plan* plan);
+/* Engine-specific, no reference counterpart: a JSON description of the plan's
+ * segments (dimension, instances, chunks, chunk kernel, the launch variant the
+ * autotuner chose and the per-variant times it measured in ms, scan kind)
+ * written to buf (truncated to len - 1 bytes, NUL-terminated); returns the
+ * length needed including the NUL. */
+size_t mgb_plan_describe(const mgb_plan* plan, char* buf, size_t len);
 mgb_status mgb_plan_destroy(mgb_plan* plan);
 
 /* Host-pointer forms (synchronous; device staging inside). carry nullable. */

@@ -4,10 +4,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -244,6 +247,10 @@ struct Segment {
     bool tiled_scan = false;
     int d = 0, nmax = 0;
     std::vector<int32_t> active;
+    // chunk-kernel launch variant (autotuner) and the times it measured
+    int variant = 0;
+    std::vector<float> tune_ms;
+    bool tuned_here = false;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -494,7 +501,8 @@ mgb_status plan_upload(PlanCore& pc, cudaStream_t st, bool synchronous) {
 mgb_status plan_streams(PlanCore& pc) {
     for (const Segment& sg : pc.segs)
         for (int mode : {MODE_LOCAL, MODE_VJP})
-            MGB_CUDA_TRY(prepare_tuned(choose_tuned(pc.plain, pc.kind, pc.rule, mode, pc.f64io != 0, sg.hi), pc.rule, mode));
+            MGB_CUDA_TRY(prepare_tuned(choose_tuned(pc.plain, pc.kind, pc.rule, mode, pc.f64io != 0, sg.hi, sg.variant),
+                                       pc.rule, mode));
     if (pc.segs.size() < 2 || pc.fork) return MGB_OK;
     MGB_CUDA_TRY(cudaEventCreateWithFlags(&pc.fork, cudaEventDisableTiming));
     for (Segment& sg : pc.segs) {
@@ -517,6 +525,129 @@ LaunchArgs seg_args(const PlanCore& pc, const Segment& sg, cudaStream_t st) {
     return la;
 }
 
+// ---------------------------------------------------------------- autotuner
+// Each chunk-kernel family has launch variants (mgb_tuned.h): k-block and CTAs
+// per SM of the tensor-core kernel, CTAs per SM (register budget) of the
+// group-tiled kernel, CTAs per SM of the generic kernel.  Before a plan's
+// first use, every variant of each segment's kernel runs the forward local
+// pass over a sample of the segment's chunks (two waves of resident CTAs,
+// spread over its instances, chunk totals written to a private buffer so no
+// caller buffer is touched) and the fastest is kept.  Results are cached for
+// the process by (family, d, rule, order bound, form).  MGB_AUTOTUNE=0 turns
+// tuning off (variant 0 everywhere); MGB_FORCE_VARIANT=k forces variant k
+// (tests use it to check every variant against the oracle).
+struct TuneKey {
+    int family, D, rule, nmax, plain, kind, f64io;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(family, D, rule, nmax, plain, kind, f64io) <
+               std::tie(o.family, o.D, o.rule, o.nmax, o.plain, o.kind, o.f64io);
+    }
+};
+struct TuneResult {
+    int variant = 0;
+    std::vector<float> ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneResult> g_tune;
+
+int env_int(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    return std::atoi(v);
+}
+
+mgb_status plan_autotune(PlanCore& pc, cudaStream_t st) {
+    const int forced = env_int("MGB_FORCE_VARIANT", -1);
+    const bool enabled = env_int("MGB_AUTOTUNE", 1) != 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (st) cudaStreamIsCapturing(st, &cap);
+    for (Segment& sg : pc.segs) {
+        const TunedChoice tc0 = choose_tuned(pc.plain, pc.kind, pc.rule, MODE_LOCAL, pc.f64io != 0, sg.hi, 0);
+        const int nv = tc0.use ? (tc0.family == 1 ? 1 : tc0.nvariants) : GENERIC_VARIANTS;
+        if (forced >= 0) {
+            sg.variant = forced < nv ? forced : 0;
+            continue;
+        }
+        if (nv <= 1 || !enabled) continue;
+        const TuneKey key{tc0.use ? tc0.family : 0, sg.d, pc.rule, sg.nmax, pc.plain ? 1 : 0, pc.kind, pc.f64io};
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            auto it = g_tune.find(key);
+            if (it != g_tune.end()) {
+                sg.variant = it->second.variant;
+                sg.tune_ms = it->second.ms;
+                continue;
+            }
+        }
+        if (cap != cudaStreamCaptureStatusNone) continue;  // no timing inside a capture
+        // sample: up to two waves of the most resident CTAs, round-robin over
+        // the segment's instances, chunk indices below csub per instance
+        const int maxctas = tc0.use ? std::max(tc0.ctas_per_sm, 2) : 8;
+        const int64_t target = std::min<int64_t>(sg.nwork, 2LL * pc.sms * maxctas);
+        const int nsub = (int)std::min<int64_t>(sg.count, target);
+        const int csub = (int)((target + nsub - 1) / nsub);
+        std::vector<InstDev> sub(pc.hi.begin() + sg.first, pc.hi.begin() + sg.first + nsub);
+        std::vector<ChunkRef> work;
+        size_t lam_doubles = 0;
+        std::vector<size_t> lam_off(nsub);
+        for (int k = 0; k < nsub; ++k) {
+            lam_off[k] = lam_doubles;
+            lam_doubles += (size_t)std::min(csub, sub[k].C) * (size_t)sub[k].n * (size_t)sub[k].m;
+        }
+        for (int c = 0; c < csub && (int64_t)work.size() < target; ++c)
+            for (int k = 0; k < nsub && (int64_t)work.size() < target; ++k)
+                if (c < sub[k].C) work.push_back(ChunkRef{k, c});
+        char* tmp = nullptr;
+        const size_t b_inst = align_up(sub.size() * sizeof(InstDev), 256);
+        const size_t b_work = align_up(work.size() * sizeof(ChunkRef), 256);
+        const size_t bytes = b_inst + b_work + lam_doubles * sizeof(double);
+        if (cudaMalloc(&tmp, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            continue;  // no room to tune: keep variant 0
+        }
+        double* lam = reinterpret_cast<double*>(tmp + b_inst + b_work);
+        for (int k = 0; k < nsub; ++k) sub[k].lam = lam + lam_off[k];
+        cudaError_t e = cudaMemcpy(tmp, sub.data(), sub.size() * sizeof(InstDev), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(tmp + b_inst, work.data(), work.size() * sizeof(ChunkRef), cudaMemcpyHostToDevice);
+        LaunchArgs la = seg_args(pc, sg, st);
+        la.insts = reinterpret_cast<const InstDev*>(tmp);
+        la.work = reinterpret_cast<const ChunkRef*>(tmp + b_inst);
+        la.nwork = (int64_t)work.size();
+        std::vector<float> ms(nv, -1.f);
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (e == cudaSuccess) e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+            cudaError_t r = launch_chunk_any(pc.plain, pc.kind, pc.rule, MODE_LOCAL, la, sg.hi, pc.sms, v);  // warm-up
+            if (r == cudaSuccess) r = cudaEventRecord(e0, st);
+            for (int rep = 0; rep < 2 && r == cudaSuccess; ++rep)
+                r = launch_chunk_any(pc.plain, pc.kind, pc.rule, MODE_LOCAL, la, sg.hi, pc.sms, v);
+            if (r == cudaSuccess) r = cudaEventRecord(e1, st);
+            if (r == cudaSuccess) r = cudaEventSynchronize(e1);
+            float t = 0.f;
+            if (r == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess) ms[v] = t / 2.f;
+            else cudaGetLastError();
+            if (r != cudaSuccess && r != cudaErrorInvalidValue && r != cudaErrorInvalidConfiguration &&
+                r != cudaErrorLaunchOutOfResources)
+                e = r;  // a sticky error: stop
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return fail(MGB_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+        if (read_clear_device_timeout()) return fail(MGB_ERR_DEVICE_TIMEOUT, "autotune: a device-side wait timed out");
+        int best = 0;
+        for (int v = 0; v < nv; ++v)
+            if (ms[v] >= 0.f && (ms[best] < 0.f || ms[v] < ms[best])) best = v;
+        sg.variant = best;
+        sg.tune_ms = ms;
+        sg.tuned_here = true;
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune[key] = TuneResult{best, ms};
+    }
+    return MGB_OK;
+}
+
 // Run f(segment, stream) for every segment: on `st` when there is one, else
 // each on its own stream, forked from and joined back into `st`.
 template <class F>
@@ -535,7 +666,7 @@ mgb_status for_segments(PlanCore& pc, cudaStream_t st, F&& f) {
 
 mgb_status seg_chunks(PlanCore& pc, Segment& sg, int mode, cudaStream_t s, const char* name) {
     const LaunchArgs la = seg_args(pc, sg, s);
-    MGB_CUDA_TRY(timed(name, s, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms); }));
+    MGB_CUDA_TRY(timed(name, s, [&] { return launch_chunk_any(pc.plain, pc.kind, pc.rule, mode, la, sg.hi, pc.sms, sg.variant); }));
     return MGB_OK;
 }
 
@@ -612,6 +743,7 @@ mgb_status run(const Call& call) {
     pc.base = static_cast<char*>(ws.base);
     plan_fill(call, pc, dv);
     st = plan_upload(pc, call.stream, false);
+    if (st == MGB_OK) st = plan_autotune(pc, call.stream);
     if (st == MGB_OK) st = plan_streams(pc);
     if (st == MGB_OK) st = call.vjp ? plan_vjp(pc, call.stream, !pc.all_ck_in) : plan_forward(pc, call.stream);
     pc.release_streams();
@@ -623,11 +755,15 @@ mgb_status run(const Call& call) {
 namespace mgb {
 // Chooses the fastest chunk kernel available for the call: the tuned
 // family when every instance has a shape it covers, else the generic one.
+int generic_ctas_per_sm(int variant) { return variant == 1 ? 4 : variant == 2 ? 2 : 8; }
+
 cudaError_t launch_chunk_any(bool plain, int kind, int rule, int mode, const LaunchArgs& a,
-                             const std::vector<InstDev>& hi, int sms) {
-    TunedChoice tc = choose_tuned(plain, kind, rule, mode, a.f64io != 0, hi);
+                             const std::vector<InstDev>& hi, int sms, int variant) {
+    TunedChoice tc = choose_tuned(plain, kind, rule, mode, a.f64io != 0, hi, variant);
     if (tc.use) return launch_tuned(tc, plain, kind, rule, mode, a, sms);
-    return launch_generic_chunk(plain, kind, rule, mode, a);
+    LaunchArgs g = a;
+    g.grid = std::max<int64_t>(1, std::min<int64_t>(a.grid, (int64_t)sms * generic_ctas_per_sm(variant % GENERIC_VARIANTS)));
+    return launch_generic_chunk(plain, kind, rule, mode, g);
 }
 }  // namespace mgb
 
@@ -667,6 +803,7 @@ mgb_status mgb_plan_create(const mgb_problem* probs, size_t count, const void* c
     P->pc.base = static_cast<char*>(base);
     plan_fill(c, P->pc, dv);
     st = plan_upload(P->pc, nullptr, true);
+    if (st == MGB_OK) st = plan_autotune(P->pc, nullptr);
     if (st == MGB_OK) st = plan_streams(P->pc);
     if (st != MGB_OK) {
         P->pc.release_streams();
@@ -692,6 +829,37 @@ mgb_status mgb_plan_vjp(mgb_plan* plan, void* stream) {
 }
 
 size_t mgb_plan_bytes(const mgb_plan* plan) { return plan ? plan->pc.bytes : 0; }
+
+size_t mgb_plan_describe(const mgb_plan* plan, char* buf, size_t len) {
+    if (!plan) return 0;
+    const PlanCore& pc = plan->pc;
+    std::string o = "{\"segments\": [";
+    char tmp[256];
+    for (size_t i = 0; i < pc.segs.size(); ++i) {
+        const Segment& sg = pc.segs[i];
+        const TunedChoice tc = choose_tuned(pc.plain, pc.kind, pc.rule, MODE_LOCAL, pc.f64io != 0, sg.hi, sg.variant);
+        const char* kernel = !tc.use ? "k_chunk" : tc.family == 1 ? "k_small" : tc.family == 2 ? "k_tile" : "k_bigtc";
+        const int ctas = !tc.use ? generic_ctas_per_sm(sg.variant % GENERIC_VARIANTS) : tc.ctas_per_sm;
+        std::snprintf(tmp, sizeof(tmp),
+                      "%s{\"d\": %d, \"instances\": %d, \"chunks\": %lld, \"kernel\": \"%s\", \"variant\": %d, "
+                      "\"ctas_per_sm\": %d, \"slots\": %lld, \"scan\": \"%s\", \"tuned_ms\": [",
+                      i ? ", " : "", sg.d, sg.count, (long long)sg.nwork, kernel, sg.variant, ctas, (long long)sg.grid,
+                      sg.tiled_scan ? "tiled" : "per-instance");
+        o += tmp;
+        for (size_t v = 0; v < sg.tune_ms.size(); ++v) {
+            std::snprintf(tmp, sizeof(tmp), "%s%.9g", v ? ", " : "", (double)sg.tune_ms[v]);
+            o += tmp;
+        }
+        o += "]}";
+    }
+    o += "]}";
+    if (buf && len) {
+        const size_t n = std::min(len - 1, o.size());
+        std::memcpy(buf, o.data(), n);
+        buf[n] = 0;
+    }
+    return o.size() + 1;
+}
 
 mgb_status mgb_plan_destroy(mgb_plan* plan) {
     g_last_error.clear();
@@ -1072,7 +1240,7 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
     la.f64io = f64io;
     la.stream = cs;
     const std::vector<InstDev> hi(1, I);
-    MGB_CUDA_TRY(launch_chunk_any(plain, p->kind, p->integrator, MODE_LOCAL, la, hi, di.sms));
+    MGB_CUDA_TRY(launch_chunk_any(plain, p->kind, p->integrator, MODE_LOCAL, la, hi, di.sms, 0));
     MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_SCAN, d_inst, 1, f64io, 0, cs));
     MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_FIN_FWD, d_inst, 1, f64io, 1, cs));
     return MGB_OK;

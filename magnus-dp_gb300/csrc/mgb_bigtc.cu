@@ -47,9 +47,9 @@ __device__ int g_device_timeout;
 namespace {
 
 constexpr int TNT = 256;
-constexpr int KB = 32;  // k-block per stage
 
-template <int D>
+// KB: k-block per stage (32 or 64; the autotuner picks)
+template <int D, int KB>
 struct TcCfg {
     static constexpr int m = D * D;
     static constexpr uint32_t TILE = D * KB * 2;              // bytes per operand piece (bf16)
@@ -148,7 +148,7 @@ __device__ __forceinline__ void split3(float x, uint16_t& p0, uint16_t& p1, uint
 // byte offset of element (row, 8-wide k chunk kc) in a K-major BF16 tile
 template <int D>
 __device__ __forceinline__ uint32_t core_off(int row, int kc) {
-    return (uint32_t)kc * TcCfg<D>::LBO + (uint32_t)(row >> 3) * TcCfg<D>::SBO + (uint32_t)(row & 7) * 16;
+    return (uint32_t)kc * (D * 16) + (uint32_t)(row >> 3) * 128 + (uint32_t)(row & 7) * 16;
 }
 
 // One k-block of an operand tile, element (row, k) = TRANS ? src[k][row] :
@@ -159,16 +159,16 @@ __device__ __forceinline__ uint32_t core_off(int row, int kc) {
 // 4-byte loads coalesced across the warp; the stores are one 16-byte chunk
 // per piece, consecutive rows at consecutive 16 bytes (no bank conflicts).
 // Plain loads: the chunk buffers are written by this kernel.
-template <int D>
+template <int D, int KB>
 struct TileRegs {
     static constexpr int NI = D * (KB / 8) / TNT;  // items per thread
     float v[NI][8];
 };
 
-template <int D, bool TRANS>
-__device__ __forceinline__ void load_tile(TileRegs<D>& r, const float* __restrict__ src, int kb) {
+template <int D, int KB, bool TRANS>
+__device__ __forceinline__ void load_tile(TileRegs<D, KB>& r, const float* __restrict__ src, int kb) {
 #pragma unroll
-    for (int i = 0; i < TileRegs<D>::NI; ++i) {
+    for (int i = 0; i < TileRegs<D, KB>::NI; ++i) {
         const int it = threadIdx.x + i * TNT, row = it % D, s8 = it / D;
         if (!TRANS) {
             const float* p = src + (int64_t)row * D + kb * KB + s8 * 8;
@@ -185,11 +185,11 @@ __device__ __forceinline__ void load_tile(TileRegs<D>& r, const float* __restric
 }
 
 // Split the held block into three BF16 pieces at t, t + TILE, t + 2 TILE.
-template <int D>
-__device__ __forceinline__ void store_tile(uint8_t* t, const TileRegs<D>& r) {
-    constexpr uint32_t TL = TcCfg<D>::TILE;
+template <int D, int KB>
+__device__ __forceinline__ void store_tile(uint8_t* t, const TileRegs<D, KB>& r) {
+    constexpr uint32_t TL = TcCfg<D, KB>::TILE;
 #pragma unroll
-    for (int i = 0; i < TileRegs<D>::NI; ++i) {
+    for (int i = 0; i < TileRegs<D, KB>::NI; ++i) {
         const int it = threadIdx.x + i * TNT, row = it % D, s8 = it / D;
         uint32_t w[3][4];
 #pragma unroll
@@ -257,16 +257,16 @@ __device__ __forceinline__ void epilogue(Pipe& pp, uint32_t s, float* __restrict
 // D*D per sample.  XT / YT: the operand's K-major tile is the transpose of
 // the stored matrix (X: element (r, k) = X[k][r]; Y: B^T element (n, k) =
 // Y[k][n] for YT, Y[n][k] otherwise).  Returns false on a time-out (uniform).
-template <int D, bool XT, bool YT>
+template <int D, int KB, bool XT, bool YT>
 __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __restrict__ Y, float* __restrict__ out,
                         bool add, int l0, int l1) {
-    using Cf = TcCfg<D>;
+    using Cf = TcCfg<D, KB>;
     constexpr int m = Cf::m;
     const int cnt = l1 - l0 + 1;
     if (cnt <= 0) return true;
-    TileRegs<D> rx, ry;
-    load_tile<D, XT>(rx, X + (int64_t)l0 * m, 0);
-    load_tile<D, YT>(ry, Y + (int64_t)l0 * m, 0);
+    TileRegs<D, KB> rx, ry;
+    load_tile<D, KB, XT>(rx, X + (int64_t)l0 * m, 0);
+    load_tile<D, KB, YT>(ry, Y + (int64_t)l0 * m, 0);
     for (int idx = 0; idx <= cnt; ++idx) {
         if (idx < cnt) {
             const int li = l0 + idx;
@@ -277,8 +277,8 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
                 uint8_t* xs = pp.stg + (size_t)b * Cf::STAGE;
                 uint8_t* ys = xs + 3 * Cf::TILE;
                 if (pp.ok) {
-                    store_tile<D>(xs, rx);
-                    store_tile<D>(ys, ry);
+                    store_tile<D, KB>(xs, rx);
+                    store_tile<D, KB>(ys, ry);
                 }
                 fence_async_smem();
                 if (__syncthreads_or(!pp.ok)) return false;
@@ -311,8 +311,8 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
                 const int nkb = kb + 1 < Cf::NKB ? kb + 1 : 0;
                 const int nli = kb + 1 < Cf::NKB ? li : li + 1;
                 if (nli <= l1) {
-                    load_tile<D, XT>(rx, X + (int64_t)nli * m, nkb);
-                    load_tile<D, YT>(ry, Y + (int64_t)nli * m, nkb);
+                    load_tile<D, KB, XT>(rx, X + (int64_t)nli * m, nkb);
+                    load_tile<D, KB, YT>(ry, Y + (int64_t)nli * m, nkb);
                 }
                 if (kb == 0 && idx > 0) epilogue<D>(pp, pp.ns - 1, out + (int64_t)(li - 1) * m, add);
             }
@@ -427,11 +427,11 @@ __device__ __forceinline__ void prefix_rev(const float* __restrict__ H, float* _
 }
 
 // ------------------------------------------------------------ the kernel
-template <int D, int RULE, int MODE>
-__global__ void __launch_bounds__(TNT, (D == 64 ? 2 : 1))
+template <int D, int KB, int RULE, int MODE, int MINB>
+__global__ void __launch_bounds__(TNT, MINB)
     k_bigtc(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work, int64_t nwork,
             float* __restrict__ scratch, int64_t slot_elems) {
-    using Cf = TcCfg<D>;
+    using Cf = TcCfg<D, KB>;
     constexpr int m = Cf::m;
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cf::BAR_OFF);
@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(TNT, (D == 64 ? 2 : 1))
             prefix_fwd<RULE>(F, Pj, keep, carry, lam, m, Kp, first, riem0, kc);
             __syncthreads();
             if (j < NL) {
-                alive = tc_pass<D, false, true>(pp, Ag, Pj, Wb, false, 0, Kp);  // W = A P
+                alive = tc_pass<D, KB, false, true>(pp, Ag, Pj, Wb, false, 0, Kp);  // W = A P
                 F = Wb;
             }
         }
@@ -500,8 +500,8 @@ __global__ void __launch_bounds__(TNT, (D == 64 ? 2 : 1))
             for (int j = n; j >= 1 && alive; --j) {
                 if (j < n) {
                     const float* Pj = tape + (int64_t)(j - 1) * Lm;
-                    alive = tc_pass<D, true, true>(pp, Ag, Gb, Hb, false, first, Kp);         // H = A^T G
-                    if (alive) alive = tc_pass<D, false, false>(pp, Gb, Pj, dAb, j < n - 1, 0, Kp);  // dA += G P^T
+                    alive = tc_pass<D, KB, true, true>(pp, Ag, Gb, Hb, false, first, Kp);         // H = A^T G
+                    if (alive) alive = tc_pass<D, KB, false, false>(pp, Gb, Pj, dAb, j < n - 1, 0, Kp);  // dA += G P^T
                     if (!alive) break;
                 }
                 prefix_rev<RULE>(j < n ? Hb : nullptr, Gb, rc + (int64_t)(j - 1) * m, m, Kp, first, riem0, kc);
@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(TNT, (D == 64 ? 2 : 1))
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(pp.tbase), "r"(Cf::NCOL) : "memory");
 }
 
-template <int D, int RULE, int MODE>
+template <int D, int KB, int RULE, int MODE, int MINB>
 cudaError_t set_attr() {
     static std::mutex mu;
     static std::vector<bool> done;
@@ -557,40 +557,56 @@ cudaError_t set_attr() {
     std::lock_guard<std::mutex> lock(mu);
     if ((int)done.size() <= dev) done.resize(dev + 1, false);
     if (done[dev]) return cudaSuccess;
-    e = cudaFuncSetAttribute(k_bigtc<D, RULE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TcCfg<D>::SMEM);
+    e = cudaFuncSetAttribute(k_bigtc<D, KB, RULE, MODE, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TcCfg<D, KB>::SMEM);
     if (e == cudaSuccess) done[dev] = true;
     return e;
 }
 
-template <int D, int RULE, int MODE>
+template <int D, int KB, int RULE, int MODE, int MINB>
 cudaError_t launch_t(const LaunchArgs& a, int grid, bool prepare_only) {
-    cudaError_t e = set_attr<D, RULE, MODE>();
+    cudaError_t e = set_attr<D, KB, RULE, MODE, MINB>();
     if (e != cudaSuccess || prepare_only) return e;
-    k_bigtc<D, RULE, MODE><<<grid, TNT, TcCfg<D>::SMEM, a.stream>>>(a.insts, a.work, a.nwork,
-                                                                    static_cast<float*>(a.scratch), a.slot_elems);
+    k_bigtc<D, KB, RULE, MODE, MINB><<<grid, TNT, TcCfg<D, KB>::SMEM, a.stream>>>(
+        a.insts, a.work, a.nwork, static_cast<float*>(a.scratch), a.slot_elems);
     return cudaGetLastError();
 }
 
-template <int D, int MODE>
+template <int D, int KB, int MODE, int MINB>
 cudaError_t launch_r(int rule, const LaunchArgs& a, int grid, bool prepare_only) {
     switch (rule) {
-        case R_BOOLE: return launch_t<D, R_BOOLE, MODE>(a, grid, prepare_only);
-        case R_SIMPSON: return launch_t<D, R_SIMPSON, MODE>(a, grid, prepare_only);
-        case R_TRAP: return launch_t<D, R_TRAP, MODE>(a, grid, prepare_only);
-        default: return launch_t<D, R_RIEMANN, MODE>(a, grid, prepare_only);
+        case R_BOOLE: return launch_t<D, KB, R_BOOLE, MODE, MINB>(a, grid, prepare_only);
+        case R_SIMPSON: return launch_t<D, KB, R_SIMPSON, MODE, MINB>(a, grid, prepare_only);
+        case R_TRAP: return launch_t<D, KB, R_TRAP, MODE, MINB>(a, grid, prepare_only);
+        default: return launch_t<D, KB, R_RIEMANN, MODE, MINB>(a, grid, prepare_only);
     }
+}
+
+template <int D, int KB, int MINB>
+cudaError_t launch_m(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only) {
+    return mode == MODE_LOCAL ? launch_r<D, KB, MODE_LOCAL, MINB>(rule, a, grid, prepare_only)
+                              : launch_r<D, KB, MODE_VJP, MINB>(rule, a, grid, prepare_only);
 }
 
 }  // namespace
 
-cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int ctas, bool prepare_only) {
+int big_variants(int D) { return D == 64 ? 4 : 2; }
+int big_ctas_per_sm(int D, int variant) { return (D == 64 && variant < 2) ? 2 : 1; }
+
+// variant: D = 64: 0 KB 32 / 2 CTAs per SM, 1 KB 64 / 2, 2 KB 32 / 1, 3 KB 64 / 1;
+//          D = 128: 0 KB 32, 1 KB 64 (one CTA per SM).
+cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, int variant, bool prepare_only) {
+    const int ctas = sms * big_ctas_per_sm(D, variant);
     int grid = (int)std::min<int64_t>(a.grid, (int64_t)ctas);
     if (grid < 1) grid = 1;
-    if (D == 128)
-        return mode == MODE_LOCAL ? launch_r<128, MODE_LOCAL>(rule, a, grid, prepare_only)
-                                  : launch_r<128, MODE_VJP>(rule, a, grid, prepare_only);
-    return mode == MODE_LOCAL ? launch_r<64, MODE_LOCAL>(rule, a, grid, prepare_only)
-                              : launch_r<64, MODE_VJP>(rule, a, grid, prepare_only);
+    if (D == 128) return variant == 1 ? launch_m<128, 64, 1>(rule, mode, a, grid, prepare_only)
+                                      : launch_m<128, 32, 1>(rule, mode, a, grid, prepare_only);
+    switch (variant) {
+        case 1: return launch_m<64, 64, 2>(rule, mode, a, grid, prepare_only);
+        case 2: return launch_m<64, 32, 1>(rule, mode, a, grid, prepare_only);
+        case 3: return launch_m<64, 64, 1>(rule, mode, a, grid, prepare_only);
+        default: return launch_m<64, 32, 2>(rule, mode, a, grid, prepare_only);
+    }
 }
 
 int read_clear_device_timeout() {

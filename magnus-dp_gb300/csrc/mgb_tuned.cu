@@ -95,8 +95,10 @@ __device__ __forceinline__ void mma_adjR(float (&acc)[4][4], const float* __rest
     }
 }
 
-template <int D, int RULE, int MODE>
-__global__ void __launch_bounds__(TNT, 2) k_tile(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work,
+// MINB: resident CTAs per SM the register allocation targets (2, or 1 with
+// up to 255 registers per thread); the autotuner picks.
+template <int D, int RULE, int MODE, int MINB>
+__global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work,
                                                  int64_t nwork, float* __restrict__ scratch, int64_t slot_elems) {
     using Cf = TileCfg<D>;
     constexpr int m = Cf::m, G = Cf::G, P4 = Cf::P4, P1 = Cf::P1, TPS = Cf::TPS, EPT = Cf::EPT;
@@ -426,7 +428,7 @@ size_t tile_smem_bytes(int) {
 
 // The dynamic shared-memory opt-in is a per-kernel, per-device setting; it is
 // made once (and can be made ahead of a stream capture by prepare_tuned).
-template <int D, int RULE, int MODE>
+template <int D, int RULE, int MODE, int MINB>
 cudaError_t set_tile_attr() {
     static std::mutex mu;
     static std::vector<bool> done;
@@ -436,45 +438,50 @@ cudaError_t set_tile_attr() {
     std::lock_guard<std::mutex> lock(mu);
     if ((int)done.size() <= dev) done.resize(dev + 1, false);
     if (done[dev]) return cudaSuccess;
-    e = cudaFuncSetAttribute(k_tile<D, RULE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_tile<D, RULE, MODE, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)tile_smem_bytes<D>(0));
     if (e == cudaSuccess) done[dev] = true;
     return e;
 }
 
-template <int D, int RULE, int MODE>
-cudaError_t launch_tile_t(const LaunchArgs& a, int nmax, int grid) {
-    const size_t smem = tile_smem_bytes<D>(nmax);
-    cudaError_t e = set_tile_attr<D, RULE, MODE>();
-    if (e != cudaSuccess) return e;
-    k_tile<D, RULE, MODE><<<grid, TNT, smem, a.stream>>>(a.insts, a.work, a.nwork, static_cast<float*>(a.scratch),
-                                                        a.slot_elems);
+template <int D, int RULE, int MODE, int MINB>
+cudaError_t launch_tile_t(const LaunchArgs& a, int grid, bool prepare_only) {
+    const size_t smem = tile_smem_bytes<D>(0);
+    cudaError_t e = set_tile_attr<D, RULE, MODE, MINB>();
+    if (e != cudaSuccess || prepare_only) return e;
+    k_tile<D, RULE, MODE, MINB><<<grid, TNT, smem, a.stream>>>(a.insts, a.work, a.nwork, static_cast<float*>(a.scratch),
+                                                              a.slot_elems);
     return cudaGetLastError();
 }
 
-template <int D, int MODE>
-cudaError_t set_tile_attr_r(int rule) {
+template <int D, int MODE, int MINB>
+cudaError_t launch_tile_r(int rule, const LaunchArgs& a, int grid, bool prepare_only) {
     switch (rule) {
-        case R_BOOLE: return set_tile_attr<D, R_BOOLE, MODE>();
-        case R_SIMPSON: return set_tile_attr<D, R_SIMPSON, MODE>();
-        case R_TRAP: return set_tile_attr<D, R_TRAP, MODE>();
-        default: return set_tile_attr<D, R_RIEMANN, MODE>();
+        case R_BOOLE: return launch_tile_t<D, R_BOOLE, MODE, MINB>(a, grid, prepare_only);
+        case R_SIMPSON: return launch_tile_t<D, R_SIMPSON, MODE, MINB>(a, grid, prepare_only);
+        case R_TRAP: return launch_tile_t<D, R_TRAP, MODE, MINB>(a, grid, prepare_only);
+        default: return launch_tile_t<D, R_RIEMANN, MODE, MINB>(a, grid, prepare_only);
     }
 }
 
-template <int D, int MODE>
-cudaError_t launch_tile_r(int rule, const LaunchArgs& a, int nmax, int grid) {
-    switch (rule) {
-        case R_BOOLE: return launch_tile_t<D, R_BOOLE, MODE>(a, nmax, grid);
-        case R_SIMPSON: return launch_tile_t<D, R_SIMPSON, MODE>(a, nmax, grid);
-        case R_TRAP: return launch_tile_t<D, R_TRAP, MODE>(a, nmax, grid);
-        default: return launch_tile_t<D, R_RIEMANN, MODE>(a, nmax, grid);
-    }
+template <int D, int MINB>
+cudaError_t launch_tile_m(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only) {
+    return mode == MODE_LOCAL ? launch_tile_r<D, MODE_LOCAL, MINB>(rule, a, grid, prepare_only)
+                              : launch_tile_r<D, MODE_VJP, MINB>(rule, a, grid, prepare_only);
 }
 
 }  // namespace
 
-TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi) {
+// variant 0: two CTAs per SM (if shared memory allows), 1: one
+cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only) {
+    if (D == 32) return variant == 0 ? launch_tile_m<32, 2>(rule, mode, a, grid, prepare_only)
+                                     : launch_tile_m<32, 1>(rule, mode, a, grid, prepare_only);
+    return variant == 0 ? launch_tile_m<16, 2>(rule, mode, a, grid, prepare_only)
+                        : launch_tile_m<16, 1>(rule, mode, a, grid, prepare_only);
+}
+
+TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, const std::vector<InstDev>& hi,
+                         int variant) {
     TunedChoice tc;
     (void)rule;
     if (hi.empty() || (mode != MODE_LOCAL && mode != MODE_VJP)) return tc;
@@ -498,7 +505,9 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
         tc.use = true;
         tc.family = 3;
         tc.D = D;
-        tc.ctas_per_sm = D == 64 ? 2 : 1;
+        tc.nvariants = big_variants(D);
+        tc.variant = variant < tc.nvariants ? variant : 0;
+        tc.ctas_per_sm = big_ctas_per_sm(D, tc.variant);
         return tc;
     }
     if (D != 16 && D != 32) return tc;
@@ -515,18 +524,19 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     tc.family = 2;
     tc.D = D;
     tc.nmax = nmax;
-    tc.ctas_per_sm = smem <= 113 * 1024 ? 2 : 1;
+    tc.nvariants = smem <= 113 * 1024 ? 2 : 1;
+    tc.variant = variant < tc.nvariants ? variant : 0;
+    if (tc.nvariants == 1) tc.variant = 1;  // one CTA per SM only
+    tc.ctas_per_sm = tc.variant == 0 ? 2 : 1;
     return tc;
 }
 
 cudaError_t prepare_tuned(const TunedChoice& tc, int rule, int mode) {
     if (!tc.use) return cudaSuccess;
-    if (tc.family == 3) {
-        LaunchArgs none{};
-        return launch_big(tc.D, rule, mode, none, 1, true);
-    }
-    if (tc.D == 32) return mode == MODE_LOCAL ? set_tile_attr_r<32, MODE_LOCAL>(rule) : set_tile_attr_r<32, MODE_VJP>(rule);
-    return mode == MODE_LOCAL ? set_tile_attr_r<16, MODE_LOCAL>(rule) : set_tile_attr_r<16, MODE_VJP>(rule);
+    LaunchArgs none{};
+    if (tc.family == 3) return launch_big(tc.D, rule, mode, none, 1, tc.variant, true);
+    if (tc.family == 2) return launch_tile(tc.D, rule, mode, none, 1, tc.variant, true);
+    return cudaSuccess;
 }
 
 SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::vector<InstDev>& hi, int64_t nwork,
@@ -539,7 +549,8 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
         Lmax = std::max(Lmax, L);
         generic = std::max<int64_t>(generic, (int64_t)(I.n + 4) * L * I.m + 7 * (int64_t)I.n * I.m);
     }
-    TunedChoice tc = choose_tuned(plain, kind, rule, MODE_VJP, f64io, hi);
+    // slots for the most resident CTAs any variant of the segment's kernel has
+    TunedChoice tc = choose_tuned(plain, kind, rule, MODE_VJP, f64io, hi, 0);
     int64_t want;
     if (tc.use && tc.family == 1) {
         sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4;  // one thread's tape
@@ -558,14 +569,10 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
 
 cudaError_t launch_tuned(const TunedChoice& tc, bool plain, int kind, int rule, int mode, const LaunchArgs& a, int sms) {
     if (tc.family == 1) return launch_small_family(plain, kind, rule, mode, a);
-    if (tc.family == 3) return launch_big(tc.D, rule, mode, a, sms * tc.ctas_per_sm, false);
+    if (tc.family == 3) return launch_big(tc.D, rule, mode, a, sms, tc.variant, false);
     int grid = (int)std::min<int64_t>(a.grid, (int64_t)sms * tc.ctas_per_sm);
     if (grid < 1) grid = 1;
-    if (tc.D == 32)
-        return mode == MODE_LOCAL ? launch_tile_r<32, MODE_LOCAL>(rule, a, tc.nmax, grid)
-                                  : launch_tile_r<32, MODE_VJP>(rule, a, tc.nmax, grid);
-    return mode == MODE_LOCAL ? launch_tile_r<16, MODE_LOCAL>(rule, a, tc.nmax, grid)
-                              : launch_tile_r<16, MODE_VJP>(rule, a, tc.nmax, grid);
+    return launch_tile(tc.D, rule, mode, a, grid, tc.variant, false);
 }
 
 }  // namespace mgb

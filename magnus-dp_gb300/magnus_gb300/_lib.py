@@ -69,6 +69,7 @@ SIGNATURES = {
     "mgb_plan_forward": (ctypes.c_int, [_VP, _VP]),
     "mgb_plan_vjp": (ctypes.c_int, [_VP, _VP]),
     "mgb_plan_bytes": (ctypes.c_size_t, [_VP]),
+    "mgb_plan_describe": (ctypes.c_size_t, [_VP, ctypes.c_char_p, ctypes.c_size_t]),
     "mgb_plan_destroy": (ctypes.c_int, [_VP]),
     "mgb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "mgb_profile_read": (ctypes.c_size_t, [ctypes.POINTER(KernelTime), ctypes.c_size_t, ctypes.c_int]),
