@@ -195,6 +195,16 @@ def _plan(lib, _lib, probs, A, out, cot=None, dA=None):
     return plan
 
 
+def _describe(lib, plan):
+    """The plan's segments: chunk kernel, the launch variant the autotuner
+    picked and the per-variant times it measured."""
+    import ctypes as ct
+    need = lib.mgb_plan_describe(plan, None, 0)
+    buf = ct.create_string_buffer(need)
+    lib.mgb_plan_describe(plan, buf, need)
+    return json.loads(buf.value.decode())["segments"]
+
+
 def _time_graph(torch, fn, steps, warmup=3):
     fn()
     torch.cuda.synchronize()
@@ -285,6 +295,7 @@ def run_config2(args):
                                             integrator=0, n=n, samples=S, dim=d, t0=0.0, tf=1.0)
     plan = _plan(lib, _lib, [mk(_lib.PRECISION_MIXED, _lib.OP_SUM)] * B, [A[i] for i in range(B)],
                  [out[i] for i in range(B)])
+    autotune = _describe(lib, plan)
     ms = _time_graph(torch, lambda: _lib.check(lib.mgb_plan_forward(plan, ct.c_void_p(torch.cuda.current_stream().cuda_stream))), args.steps)
     lib.mgb_plan_destroy(plan)
     sub = 4
@@ -310,7 +321,7 @@ def run_config2(args):
                       "precision": "mixed", "fp32_simt": {"achieved_tflops": tf, "nominal_peak_tflops": fp32_peak,
                                                           "frac": tf / fp32_peak},
                       "plain_fp64": {"value": sub * S * n / (res[_lib.PRECISION_PLAIN][1] / 1e3), "instances": sub},
-                      "rel_err_per_order_vs_fp64": errs}))
+                      "rel_err_per_order_vs_fp64": errs, "autotune": autotune}))
 
 
 def run_config3(args):
@@ -454,6 +465,7 @@ def main():
     # a step = plan forward + plan VJP, captured once into a CUDA graph.
     plan = ctypes.c_void_p()
     _lib.check(lib.mgb_plan_create(probs, B, ptrs(A), ptrs(out), ptrs(cot), ptrs(dA), ctypes.byref(plan)))
+    autotune = _describe(lib, plan)
     stream = torch.cuda.current_stream(dev)
     sptr = ctypes.c_void_p(stream.cuda_stream)
 
@@ -532,7 +544,8 @@ def main():
                                      f"sum, float32 in, fwd+VJP, checkpoints every {c['K']} samples",
                          "precision": args.precision, "global_batch": B * world,
                          "cache": "inputs 68.7 GB >> L2 (no flush needed)",
-                         "execution": "mgb_plan forward+VJP captured in one CUDA graph, replayed per step"},
+                         "execution": "mgb_plan forward+VJP captured in one CUDA graph, replayed per step",
+                         "autotune": autotune},
               "roofline": roof, "gpu_launches": launches, "clocks": clk,
               "kernels_ms_per_step": {k: v[1] / args.steps for k, v in kernels.items()}}
 
@@ -550,6 +563,8 @@ def main():
         def sp(t):
             return (ctypes.c_void_p * sub)(*[t[i].data_ptr() for i in range(sub)])
 
+        # untimed warm-up: the first call of a shape runs the autotuner
+        _lib.check(lib.mgb_forward_batched(probs_p, sub, sp(Ap), sp(out_p), None, sptr))
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
@@ -582,15 +597,21 @@ def main():
         torch.cuda.empty_cache()
         A_dev = torch.empty((eb, S, d, d), dtype=torch.float32, device=dev)
 
+        marks = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
         def e2e_step():
+            marks[0].record(stream)
             A_dev.copy_(A_host, non_blocking=True)
             x = A_dev.detach().requires_grad_(True)
             g = cot_host.to(dev, non_blocking=True)
+            marks[1].record(stream)
             o = magnus(x, n, c["t0"], c["tf"], op="sum", integrator="Boole", precision=args.precision,
                        checkpoint_K=c["K"])
             o.backward(g)
+            marks[2].record(stream)
             out_host.copy_(o.detach(), non_blocking=True)
             dA_host.copy_(x.grad, non_blocking=True)
+            marks[3].record(stream)
 
         e2e_step()
         torch.cuda.synchronize()
@@ -605,9 +626,11 @@ def main():
         e2e_ms = g0.elapsed_time(g1) / e2e_steps
         h2d = A_host.numel() * 4 + cot_host.numel() * 4
         d2h = dA_host.numel() * 4 + out_host.numel() * 4
+        split = [marks[i].elapsed_time(marks[i + 1]) for i in range(3)]  # last step
         result["e2e"] = {"value": eb * S * n / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "instances": eb, "ms_per_step": e2e_ms,
-                         "api": "magnus_gb300.autograd.magnus forward + backward"}
+                         "api": "magnus_gb300.autograd.magnus forward + backward",
+                         "last_step_ms": {"h2d": split[0], "compute": split[1], "d2h": split[2]}}
 
         # ---- CPU baseline (oracle port on the host cores, bounded sample)
         threads = os.cpu_count() or 1
