@@ -132,6 +132,20 @@ mgb_status mgb_plan_destroy(mgb_plan* plan);
 mgb_status mgb_forward_host(const mgb_problem* p, const void* A, void* out, void* carry);
 mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, void* dA);
 
+/* Engine-specific (the reference makes one compute(record_vjp=True) and one
+ * compute_vjp(vjp_data) call per instance, src/api/pybind.cpp:357-433): the
+ * forward (out) and the VJP (dA) of `count` instances from HOST buffers in
+ * one synchronous call.  Instances go to the device in sub-batches
+ * (MGB_HOST_SUBBATCHES, default 4, of at least 256 MB each) through three
+ * rotating device slots, so the host-to-device copy of one sub-batch, the
+ * kernels of the previous one and the device-to-host copy of the one before
+ * overlap.  Host buffers should be page-locked (cudaMallocHost /
+ * cudaHostRegister / torch pin_memory) for the copies to overlap; pageable
+ * ones are correct but staged by the driver.  The slots stay allocated on
+ * the device for later calls (calls are serialized inside the library). */
+mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, const void* const* A,
+                                    const void* const* cot, void* const* out, void* const* dA);
+
 /* Forward that allocates no device memory.  For callers that cannot call
  * cudaMalloc during their work — an XLA/JAX custom call, or any framework
  * whose caching allocator already holds the GPU's memory, or a host that must

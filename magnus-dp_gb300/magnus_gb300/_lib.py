@@ -59,6 +59,7 @@ SIGNATURES = {
     "mgb_vjp_batched": (ctypes.c_int, [_PP, ctypes.c_size_t, _VP, _VP, _VP, _VP, _VP]),
     "mgb_forward_host": (ctypes.c_int, [_PP, _VP, _VP, _VP]),
     "mgb_vjp_host": (ctypes.c_int, [_PP, _VP, _VP, _VP]),
+    "mgb_fwd_vjp_host_batched": (ctypes.c_int, [_PP, ctypes.c_size_t, _VP, _VP, _VP, _VP]),
     "mgb_set_gl_table": (ctypes.c_int, [ctypes.c_size_t, _VP, _VP]),
     "mgb_max_order": (ctypes.c_size_t, []),
     "mgb_device_check": (ctypes.c_int, []),
