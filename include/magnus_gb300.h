@@ -55,7 +55,12 @@ typedef enum mgb_status {
 } mgb_status;
 
 enum { MGB_KIND_MATRIX = 0, MGB_KIND_SPACECURVE = 1 };
-enum { MGB_DTYPE_F32 = 0, MGB_DTYPE_F64 = 1 };
+/* C64 / C128: interleaved (re, im) pairs of float / double; matrix kind only
+ * (a complex d x d problem runs as the real 2d x 2d problem on
+ * [[Re A, -Im A], [Im A, Re A]]; the VJP is the reference's bilinear one).
+ * Complex problems go through the one-shot entry points (not plans, not
+ * mgb_forward_noalloc, not mgb_fwd_vjp_host_batched). */
+enum { MGB_DTYPE_F32 = 0, MGB_DTYPE_F64 = 1, MGB_DTYPE_C64 = 2, MGB_DTYPE_C128 = 3 };
 /* PLAIN: every product and sum in FP64 (parity form, <=1e-12 vs the reference).
  * MIXED: per-sample products and in-chunk prefixes in FP32, chunk carries,
  *        scans and the final Omega assembly in FP64. */

@@ -106,6 +106,18 @@ DevInfo device_info() {
 }
 
 // ---------------------------------------------------------------- validation
+bool is_complex(int32_t dtype) { return dtype == MGB_DTYPE_C64 || dtype == MGB_DTYPE_C128; }
+
+// The real problem a complex one runs as (dimension 2d, real parts' type).
+mgb_problem real_problem(const mgb_problem& p) {
+    mgb_problem r = p;
+    if (is_complex(p.dtype)) {
+        r.dtype = p.dtype == MGB_DTYPE_C128 ? MGB_DTYPE_F64 : MGB_DTYPE_F32;
+        r.dim = 2 * p.dim;
+    }
+    return r;
+}
+
 struct Derived {
     int m, Q, C, K, div;
     int64_t nm;
@@ -138,8 +150,12 @@ mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
     if (p->n == 0) return fail(MGB_ERR_INVALID_ARGUMENT, "n must be at least 1");
     if (p->kind != MGB_KIND_MATRIX && p->kind != MGB_KIND_SPACECURVE)
         return fail(MGB_ERR_INVALID_ARGUMENT, "invalid dispatch option (based on params)");
-    if (p->dtype != MGB_DTYPE_F32 && p->dtype != MGB_DTYPE_F64)
+    if (p->dtype != MGB_DTYPE_F32 && p->dtype != MGB_DTYPE_F64 && p->dtype != MGB_DTYPE_C64 &&
+        p->dtype != MGB_DTYPE_C128)
         return fail(MGB_ERR_TYPE, "magnus only supports dtypes float32, float64, complex64, and complex128");
+    if (is_complex(p->dtype) && p->kind == MGB_KIND_SPACECURVE)
+        return fail(MGB_ERR_TYPE, "complex spacecurve inputs are not supported by the GB300 engine");
+    if (is_complex(p->dtype) && p->dim > 2048) return fail(MGB_ERR_INVALID_ARGUMENT, "matrix dimension is too large");
     if (p->precision != MGB_PRECISION_PLAIN && p->precision != MGB_PRECISION_MIXED)
         return fail(MGB_ERR_INVALID_ARGUMENT, "invalid dispatch option (based on params)");
     if (p->op < MGB_OP_ONE || p->op > MGB_OP_SUM)
@@ -295,6 +311,9 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     for (size_t i = 0; i < call.count; ++i) {
         mgb_status st = validate(&call.probs[i], gl->max_order, &dv[i]);
         if (st != MGB_OK) return st;
+        if (is_complex(call.probs[i].dtype))
+            return fail(MGB_ERR_INVALID_ARGUMENT,
+                        "complex problems run through mgb_forward / mgb_vjp and their batched and host forms");
         const mgb_problem& p = call.probs[i];
         if (p.kind != p0.kind || p.dtype != p0.dtype || p.precision != p0.precision || p.integrator != p0.integrator)
             return fail(MGB_ERR_INVALID_ARGUMENT, "batched instances must share kind, dtype, precision and integrator");
@@ -731,8 +750,11 @@ mgb_status plan_vjp(PlanCore& pc, cudaStream_t st, bool recompute) {
 }
 
 // One-shot call: plan in stream-ordered memory, run, release.
+mgb_status run_complex(const Call& call);
+
 mgb_status run(const Call& call) {
     if (call.count == 0) return MGB_OK;
+    if (call.probs && is_complex(call.probs[0].dtype)) return run_complex(call);
     PlanCore pc;
     std::vector<Derived> dv;
     mgb_status st = plan_layout(call, pc, dv);
@@ -748,6 +770,92 @@ mgb_status run(const Call& call) {
     if (st == MGB_OK) st = call.vjp ? plan_vjp(pc, call.stream, !pc.all_ck_in) : plan_forward(pc, call.stream);
     pc.release_streams();
     return st;
+}
+
+// Complex problems: expand the inputs to the real 2d x 2d form
+// (launch_cplx_embed), run the real problems, and read the outputs back
+// (launch_cplx_extract).  Checkpoint buffers are the real problems' own.
+mgb_status run_complex(const Call& call) {
+    const size_t count = call.count;
+    for (size_t i = 0; i < count; ++i) {
+        Derived dv;
+        mgb_status st = validate(&call.probs[i], gl_snapshot()->max_order, &dv);
+        if (st != MGB_OK) return st;
+        if (call.probs[i].dtype != call.probs[0].dtype)
+            return fail(MGB_ERR_INVALID_ARGUMENT, "batched instances must share kind, dtype, precision and integrator");
+    }
+    if (!call.A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+    const bool f64 = call.probs[0].dtype == MGB_DTYPE_C128;
+    const size_t es = f64 ? 8 : 4;  // bytes per real part
+    std::vector<mgb_problem> rp(count);
+    std::vector<size_t> off_a(count), off_o(count), off_c(count), off_k(count), off_g(count);
+    size_t bytes = 0;
+    for (size_t i = 0; i < count; ++i) {
+        const mgb_problem& p = call.probs[i];
+        if (!call.A[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+        rp[i] = real_problem(p);
+        const size_t m4 = 4 * (size_t)p.dim * p.dim;  // real elements of one 2d x 2d matrix
+        const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
+        const size_t Q = p.n > 1 ? (size_t)(p.n + 3) / 2 : 1;
+        off_a[i] = bytes; bytes = align_up(bytes + (size_t)p.samples * m4 * es, 256);
+        off_o[i] = bytes; bytes = align_up(bytes + nout * m4 * es, 256);
+        off_c[i] = bytes;
+        if (!call.vjp && call.carry && call.carry[i] && p.n > 1)
+            bytes = align_up(bytes + Q * (size_t)(p.n - 1) * (size_t)p.samples * m4 * es, 256);
+        off_k[i] = bytes;
+        if (call.vjp) bytes = align_up(bytes + nout * m4 * es, 256);
+        off_g[i] = bytes;
+        if (call.vjp) bytes = align_up(bytes + (size_t)p.samples * m4 * es, 256);
+    }
+    cudaStream_t st = call.stream;
+    Workspace ws;
+    ws.st = st;
+    MGB_CUDA_TRY(cudaMallocAsync(&ws.base, bytes, st));
+    char* base = static_cast<char*>(ws.base);
+    std::vector<const void*> rA(count), rcot(count);
+    std::vector<void*> rout(count), rcarry(count, nullptr), rdA(count);
+    for (size_t i = 0; i < count; ++i) {
+        const mgb_problem& p = call.probs[i];
+        const int d = (int)p.dim;
+        const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
+        rA[i] = base + off_a[i];
+        rout[i] = base + off_o[i];
+        MGB_CUDA_TRY(launch_cplx_embed(f64, call.A[i], base + off_a[i], (int64_t)p.samples, d, false, st));
+        if (call.vjp) {
+            if (!call.cot || !call.cot[i] || !call.dA || !call.dA[i])
+                return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
+            rcot[i] = base + off_k[i];
+            rdA[i] = base + off_g[i];
+            MGB_CUDA_TRY(launch_cplx_embed(f64, call.cot[i], base + off_k[i], (int64_t)nout, d, true, st));
+        } else if (call.carry && call.carry[i] && p.n > 1) {
+            rcarry[i] = base + off_c[i];
+        }
+    }
+    Call rc = call;
+    rc.probs = rp.data();
+    rc.A = rA.data();
+    rc.out = call.vjp ? nullptr : rout.data();
+    rc.carry = (!call.vjp && call.carry) ? rcarry.data() : nullptr;
+    rc.cot = call.vjp ? rcot.data() : nullptr;
+    rc.dA = call.vjp ? rdA.data() : nullptr;
+    mgb_status s = run(rc);
+    if (s != MGB_OK) return s;
+    for (size_t i = 0; i < count; ++i) {
+        const mgb_problem& p = call.probs[i];
+        const int d = (int)p.dim;
+        const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
+        const size_t Q = p.n > 1 ? (size_t)(p.n + 3) / 2 : 1;
+        if (call.vjp) {
+            MGB_CUDA_TRY(launch_cplx_extract(f64, rdA[i], call.dA[i], (int64_t)p.samples, d, true, st));
+        } else {
+            if (!call.out || !call.out[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
+            MGB_CUDA_TRY(launch_cplx_extract(f64, rout[i], call.out[i], (int64_t)nout, d, false, st));
+            if (rcarry[i])
+                MGB_CUDA_TRY(launch_cplx_extract(f64, rcarry[i], call.carry[i],
+                                                 (int64_t)(Q * (size_t)(p.n - 1) * (size_t)p.samples), d, false, st));
+        }
+    }
+    return MGB_OK;
 }
 
 }  // namespace
@@ -959,6 +1067,12 @@ size_t mgb_checkpoint_bytes(const mgb_problem* p) {
     Derived dv;
     std::string saved = g_last_error;
     mgb_status st = validate(p, gl_snapshot()->max_order, &dv);
+    if (st == MGB_OK && is_complex(p->dtype)) {  // the checkpoints of the real problem it runs as
+        const mgb_problem r = real_problem(*p);
+        st = validate(&r, gl_snapshot()->max_order, &dv);
+        g_last_error = saved;
+        return st == MGB_OK ? ckpt_doubles(r, dv) * sizeof(double) : 0;
+    }
     g_last_error = saved;
     if (st != MGB_OK) return 0;
     return ckpt_doubles(*p, dv) * sizeof(double);
@@ -994,7 +1108,9 @@ mgb_status mgb_vjp_batched(const mgb_problem* probs, size_t count, const void* c
     return run(c);
 }
 
-static size_t elem_size(const mgb_problem* p) { return p->dtype == MGB_DTYPE_F64 ? 8 : 4; }
+static size_t elem_size(const mgb_problem* p) {
+    return p->dtype == MGB_DTYPE_C128 ? 16 : (p->dtype == MGB_DTYPE_F64 || p->dtype == MGB_DTYPE_C64) ? 8 : 4;
+}
 
 static void sizes_of(const mgb_problem* p, size_t* in_elems, size_t* out_elems, size_t* carry_elems) {
     const size_t m = p->kind == MGB_KIND_SPACECURVE ? 4 : (size_t)(p->dim * p->dim);
@@ -1384,6 +1500,8 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
     Derived v;
     mgb_status st = validate(p, gl->max_order, &v);
     if (st != MGB_OK) return st;
+    if (is_complex(p->dtype))
+        return fail(MGB_ERR_INVALID_ARGUMENT, "complex problems run through mgb_forward / mgb_vjp and their batched and host forms");
     if (!A) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
     if (!out) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
     cudaStream_t cs = static_cast<cudaStream_t>(stream);

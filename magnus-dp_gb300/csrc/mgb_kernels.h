@@ -36,6 +36,13 @@ cudaError_t launch_small(bool fp64, int kind, int which, const InstDev* insts, i
 // by chunk count (descending); active[c] = number of them with C > c.  The
 // forward pass writes pi^0..pi^C; the reverse pass rho^{C-1}..rho^0 (from
 // tau) and zeroes the dA rows shared by two chunks.
+// Complex matrix problems as real 2d x 2d problems (mgb_complex.cu): count
+// complex d x d matrices (interleaved re, im; float or double parts) to
+// [[X, -Y], [Y, X]] (cot: the cotangent form [[Re C, Im C], [-Im C, Re C]] / 2),
+// and back (grad: the bilinear gradient (dR11 + dR22) + i (dR12 - dR21)).
+cudaError_t launch_cplx_embed(bool f64, const void* Z, void* out, int64_t count, int d, bool cot, cudaStream_t st);
+cudaError_t launch_cplx_extract(bool f64, const void* in, void* Z, int64_t count, int d, bool grad, cudaStream_t st);
+
 bool scan_tiled_ok(int kind, int d);
 cudaError_t launch_scan_tiled(const InstDev* insts, int count, int d, int nmax, const std::vector<int32_t>& active,
                               bool reverse, int f64io, cudaStream_t st);

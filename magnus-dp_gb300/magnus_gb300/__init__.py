@@ -21,8 +21,10 @@ Differences from the reference, by design:
 * ``compute_vjp(vjp_data=...)`` checks the carry's shape exactly like the
   reference and then recomputes what it needs from the chunk checkpoints
   (replaying the forward costs less than reading Q*(n-1)*S*d*d values).
-* complex64 / complex128 inputs are rejected with ValueError("invalid
-  dispatch option ...") for now.
+* complex64 / complex128 matrix data run as the real problem of twice the
+  dimension on [[Re A, -Im A], [Im A, Re A]] (exact: the map is an algebra
+  homomorphism); the VJP is the reference's bilinear one.  Complex
+  SpaceCurve data raise TypeError.
 """
 from __future__ import annotations
 
@@ -144,8 +146,10 @@ def _dtype_code(dtype) -> int:
         return _lib.DTYPE_F32
     if dtype == np.float64:
         return _lib.DTYPE_F64
-    if dtype in (np.complex64, np.complex128):
-        raise ValueError(_INVALID + ": complex dtypes are not available on the GB300 engine yet")
+    if dtype == np.complex64:
+        return _lib.DTYPE_C64
+    if dtype == np.complex128:
+        return _lib.DTYPE_C128
     raise TypeError("magnus only supports dtypes float32, float64, complex64, and complex128")
 
 

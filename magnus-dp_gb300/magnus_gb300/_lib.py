@@ -14,7 +14,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libmagnus_gb300.so")
 
 KIND_MATRIX, KIND_SPACECURVE = 0, 1
-DTYPE_F32, DTYPE_F64 = 0, 1
+DTYPE_F32, DTYPE_F64, DTYPE_C64, DTYPE_C128 = 0, 1, 2, 3
 PRECISION_PLAIN, PRECISION_MIXED = 0, 1
 OP_ONE, OP_MANY, OP_SUM = 0, 1, 2
 INTEGRATOR_CODES = {"Boole": 0, "Simpson": 1, "Trapezoid": 2, "Riemann": 3}

@@ -21,7 +21,8 @@ import torch
 
 from . import _lib
 
-_DTYPES = {torch.float32: _lib.DTYPE_F32, torch.float64: _lib.DTYPE_F64}
+_DTYPES = {torch.float32: _lib.DTYPE_F32, torch.float64: _lib.DTYPE_F64, torch.complex64: _lib.DTYPE_C64,
+           torch.complex128: _lib.DTYPE_C128}
 
 
 def _problems(A, n, t0, tf, op, integrator, precision, kind, checkpoint_K):
@@ -85,13 +86,20 @@ class MagnusFunction(torch.autograd.Function):
         Ab, ck = ctx.saved_tensors
         batched, prob = ctx.meta
         B = Ab.shape[0]
-        g = (grad_out if batched else grad_out.unsqueeze(0)).to(Ab.dtype).contiguous()
+        g = (grad_out if batched else grad_out.unsqueeze(0)).to(Ab.dtype)
+        if Ab.is_complex():
+            # torch passes and expects conjugate-Wirtinger gradients; the
+            # engine's VJP is the bilinear J^T c, so grad_A = conj(J^T conj(g))
+            g = g.conj()
+        g = g.resolve_conj().contiguous()
         dA = torch.empty_like(Ab)
         lib = _lib.load()
         probs = (_lib.Problem * B)(*([prob] * B))
         _lib.check(lib.mgb_vjp_batched(probs, B, _ptr_array([Ab[i] for i in range(B)]),
                                        _ptr_array([g[i] for i in range(B)]), _ptr_array([ck[i] for i in range(B)]),
                                        _ptr_array([dA[i] for i in range(B)]), _stream()))
+        if Ab.is_complex():
+            dA = dA.conj().resolve_conj()
         dA = dA if batched else dA[0]
         return dA, None, None, None, None, None, None, None, None
 

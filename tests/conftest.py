@@ -43,8 +43,11 @@ def load_cases(name):
 
 
 def rel(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    """Relative Frobenius distance ||a - b|| / ||b|| (complex-aware)."""
+    a, b = np.asarray(a), np.asarray(b)
+    t = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a = a.astype(t)
+    b = b.astype(t)
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
 

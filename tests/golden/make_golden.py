@@ -119,6 +119,43 @@ def float32_cases():
     return cases
 
 
+def complex_cases():
+    """Complex matrix problems (the reference's complex64 / complex128
+    kernels): forward, bilinear VJP, one carry record, and a complex64 run
+    next to the complex128 run on the upcast input."""
+    rng = np.random.default_rng(11)
+    cases = {}
+    idx = 0
+    for integ, S in [("Boole", 17), ("Simpson", 13), ("Trapezoid", 11), ("Riemann", 10)]:
+        for d in (2, 3):
+            A = (rng.standard_normal((S, d, d)) + 1j * rng.standard_normal((S, d, d))) / np.sqrt(2 * d)
+            for n in (1, 3, 5):
+                for op in ("one", "many", "sum"):
+                    key = f"c{idx:03d}"
+                    idx += 1
+                    out = core.compute(n, A, 0.0, 1.3, op=op, matrix_backend=backend(d), integrator=integ,
+                                       gl_backend="serial")
+                    cot = rng.standard_normal(out.shape) + 1j * rng.standard_normal(out.shape)
+                    dA = core.compute_vjp(n, A, cot, t0=0.0, tf=1.3, op=op, matrix_backend=backend(d),
+                                          integrator=integ)
+                    cases[key] = dict(kind="matrix", integrator=integ, op=op, n=n, t0=0.0, tf=1.3, A=A, out=out,
+                                      cot=cot, dA=dA)
+            _, carry = core.compute(4, A, 0.0, 1.3, op="sum", matrix_backend=backend(d), integrator=integ,
+                                    gl_backend="serial", record_vjp=True)
+            out = core.compute(4, A, 0.0, 1.3, op="sum", matrix_backend=backend(d), integrator=integ,
+                               gl_backend="serial")
+            cases[f"carry_{integ}_{d}"] = dict(kind="matrix", integrator=integ, op="sum", n=4, t0=0.0, tf=1.3, A=A,
+                                               out=out, carry=carry)
+    A64 = (rng.standard_normal((129, 4, 4)) + 1j * rng.standard_normal((129, 4, 4))) / 3
+    A32 = A64.astype(np.complex64)
+    out32 = core.compute(5, A32, 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole", gl_backend="serial")
+    out64 = core.compute(5, A32.astype(np.complex128), 0.0, 1.0, op="many", matrix_backend="Manual",
+                         integrator="Boole", gl_backend="serial")
+    cases["c64"] = dict(kind="matrix", integrator="Boole", op="many", n=5, t0=0.0, tf=1.0, A=A32, out=out32,
+                        out64=out64)
+    return cases
+
+
 def save(name, cases):
     flat = {}
     for key, c in cases.items():
@@ -128,10 +165,10 @@ def save(name, cases):
 
 
 def main():
-    save("small.npz", small_cases())
-    save("medium.npz", medium_cases())
-    save("config0.npz", config0_cases())
-    save("float32.npz", float32_cases())
+    makers = {"small.npz": small_cases, "medium.npz": medium_cases, "config0.npz": config0_cases,
+              "float32.npz": float32_cases, "complex.npz": complex_cases}
+    for name in (sys.argv[1:] or makers):  # e.g. `make_golden.py complex.npz` regenerates one file
+        save(name, makers[name]())
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -90,3 +90,33 @@ def test_oracle_batch_threads_match_serial():
         np.testing.assert_array_equal(fwd[b].reshape(4, 2, 2), O.forward(A[b], 4, 0.0, 1.0, "many", "Boole"))
         np.testing.assert_array_equal(vjp[b].reshape(33, 2, 2),
                                       O.vjp(A[b], cot[b], 4, 0.0, 1.0, "sum", "Boole"))
+
+
+def _embed(Z):
+    """Complex (..., d, d) -> real (..., 2d, 2d) [[X, -Y], [Y, X]]."""
+    X, Y = Z.real, Z.imag
+    return np.concatenate([np.concatenate([X, -Y], -1), np.concatenate([Y, X], -1)], -2)
+
+
+def test_complex_embedding_reproduces_reference():
+    """The GB300 engine runs a complex d x d problem as the real 2d x 2d
+    problem on [[Re A, -Im A], [Im A, Re A]], with the cotangent
+    [[Re C, Im C], [-Im C, Re C]] / 2 and dA = (dR11 + dR22) + i (dR12 - dR21).
+    Checked here with the oracle on the embedded problems against the
+    reference's complex128 outputs (forward, bilinear VJP, carry record)."""
+    cases = load_cases("complex.npz")
+    for key, c in cases.items():
+        if key == "c64":
+            continue
+        A, n, op, integ = c["A"], int(c["n"]), str(c["op"]), str(c["integrator"])
+        d = A.shape[-1]
+        AR = _embed(A)
+        outR = O.forward(AR, n, float(c["t0"]), float(c["tf"]), op, integ)
+        out = outR[..., :d, :d] + 1j * outR[..., d:, :d]
+        assert rel(out, c["out"]) <= 1e-13, key
+        if "dA" in c:
+            C = c["cot"]
+            RC = np.concatenate([np.concatenate([C.real, C.imag], -1), np.concatenate([-C.imag, C.real], -1)], -2) / 2
+            dR = O.vjp(AR, RC, n, float(c["t0"]), float(c["tf"]), op, integ)
+            G = (dR[:, :d, :d] + dR[:, d:, d:]) + 1j * (dR[:, :d, d:] - dR[:, d:, :d])
+            assert rel(G, c["dA"]) <= 1e-13, key
