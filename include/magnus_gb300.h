@@ -55,11 +55,13 @@ typedef enum mgb_status {
 } mgb_status;
 
 enum { MGB_KIND_MATRIX = 0, MGB_KIND_SPACECURVE = 1 };
-/* C64 / C128: interleaved (re, im) pairs of float / double; matrix kind only
- * (a complex d x d problem runs as the real 2d x 2d problem on
- * [[Re A, -Im A], [Im A, Re A]]; the VJP is the reference's bilinear one).
- * Complex problems go through the one-shot entry points (not plans, not
- * mgb_forward_noalloc, not mgb_fwd_vjp_host_batched). */
+/* C64 / C128: interleaved (re, im) pairs of float / double.  A complex d x d
+ * matrix problem runs as the real 2d x 2d problem on [[Re A, -Im A],
+ * [Im A, Re A]]; complex SpaceCurve data as the real 8 x 8 problem on the
+ * embedding of the quaternion right-multiplication matrix of (0, f); the VJP
+ * is the reference's bilinear one.  Complex problems go through the
+ * one-shot entry points (not plans, not mgb_forward_noalloc, not
+ * mgb_fwd_vjp_host_batched). */
 enum { MGB_DTYPE_F32 = 0, MGB_DTYPE_F64 = 1, MGB_DTYPE_C64 = 2, MGB_DTYPE_C128 = 3 };
 /* PLAIN: every product and sum in FP64 (parity form, <=1e-12 vs the reference).
  * MIXED: per-sample products and in-chunk prefixes in FP32, chunk carries,

@@ -109,11 +109,19 @@ DevInfo device_info() {
 bool is_complex(int32_t dtype) { return dtype == MGB_DTYPE_C64 || dtype == MGB_DTYPE_C128; }
 
 // The real problem a complex one runs as (dimension 2d, real parts' type).
+// Complex SpaceCurve data run as the real 8 x 8 matrix problem with op many
+// (mgb_complex.cu); complex matrix data as the real 2d x 2d problem.
 mgb_problem real_problem(const mgb_problem& p) {
     mgb_problem r = p;
     if (is_complex(p.dtype)) {
         r.dtype = p.dtype == MGB_DTYPE_C128 ? MGB_DTYPE_F64 : MGB_DTYPE_F32;
-        r.dim = 2 * p.dim;
+        if (p.kind == MGB_KIND_SPACECURVE) {
+            r.kind = MGB_KIND_MATRIX;
+            r.dim = 8;
+            r.op = MGB_OP_MANY;
+        } else {
+            r.dim = 2 * p.dim;
+        }
     }
     return r;
 }
@@ -153,8 +161,6 @@ mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
     if (p->dtype != MGB_DTYPE_F32 && p->dtype != MGB_DTYPE_F64 && p->dtype != MGB_DTYPE_C64 &&
         p->dtype != MGB_DTYPE_C128)
         return fail(MGB_ERR_TYPE, "magnus only supports dtypes float32, float64, complex64, and complex128");
-    if (is_complex(p->dtype) && p->kind == MGB_KIND_SPACECURVE)
-        return fail(MGB_ERR_TYPE, "complex spacecurve inputs are not supported by the GB300 engine");
     if (is_complex(p->dtype) && p->dim > 2048) return fail(MGB_ERR_INVALID_ARGUMENT, "matrix dimension is too large");
     if (p->precision != MGB_PRECISION_PLAIN && p->precision != MGB_PRECISION_MIXED)
         return fail(MGB_ERR_INVALID_ARGUMENT, "invalid dispatch option (based on params)");
@@ -794,8 +800,8 @@ mgb_status run_complex(const Call& call) {
         const mgb_problem& p = call.probs[i];
         if (!call.A[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
         rp[i] = real_problem(p);
-        const size_t m4 = 4 * (size_t)p.dim * p.dim;  // real elements of one 2d x 2d matrix
-        const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
+        const size_t m4 = (size_t)rp[i].dim * rp[i].dim;  // real elements of one matrix of the real problem
+        const size_t nout = rp[i].op == MGB_OP_MANY ? (size_t)p.n : 1;
         const size_t Q = p.n > 1 ? (size_t)(p.n + 3) / 2 : 1;
         off_a[i] = bytes; bytes = align_up(bytes + (size_t)p.samples * m4 * es, 256);
         off_o[i] = bytes; bytes = align_up(bytes + nout * m4 * es, 256);
@@ -816,17 +822,20 @@ mgb_status run_complex(const Call& call) {
     std::vector<void*> rout(count), rcarry(count, nullptr), rdA(count);
     for (size_t i = 0; i < count; ++i) {
         const mgb_problem& p = call.probs[i];
+        const bool sc = p.kind == MGB_KIND_SPACECURVE;
         const int d = (int)p.dim;
         const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
         rA[i] = base + off_a[i];
         rout[i] = base + off_o[i];
-        MGB_CUDA_TRY(launch_cplx_embed(f64, call.A[i], base + off_a[i], (int64_t)p.samples, d, false, st));
+        if (sc) MGB_CUDA_TRY(launch_sc_complex(SC_EMBED, f64, call.A[i], base + off_a[i], (int64_t)p.samples, (int)p.n, p.op, st));
+        else MGB_CUDA_TRY(launch_cplx_embed(f64, call.A[i], base + off_a[i], (int64_t)p.samples, d, false, st));
         if (call.vjp) {
             if (!call.cot || !call.cot[i] || !call.dA || !call.dA[i])
                 return fail(MGB_ERR_INVALID_ARGUMENT, "input buffer must not be null");
             rcot[i] = base + off_k[i];
             rdA[i] = base + off_g[i];
-            MGB_CUDA_TRY(launch_cplx_embed(f64, call.cot[i], base + off_k[i], (int64_t)nout, d, true, st));
+            if (sc) MGB_CUDA_TRY(launch_sc_complex(SC_COT, f64, call.cot[i], base + off_k[i], 0, (int)p.n, p.op, st));
+            else MGB_CUDA_TRY(launch_cplx_embed(f64, call.cot[i], base + off_k[i], (int64_t)nout, d, true, st));
         } else if (call.carry && call.carry[i] && p.n > 1) {
             rcarry[i] = base + off_c[i];
         }
@@ -845,14 +854,19 @@ mgb_status run_complex(const Call& call) {
         const int d = (int)p.dim;
         const size_t nout = p.op == MGB_OP_MANY ? (size_t)p.n : 1;
         const size_t Q = p.n > 1 ? (size_t)(p.n + 3) / 2 : 1;
+        const bool sc = p.kind == MGB_KIND_SPACECURVE;
         if (call.vjp) {
-            MGB_CUDA_TRY(launch_cplx_extract(f64, rdA[i], call.dA[i], (int64_t)p.samples, d, true, st));
+            if (sc) MGB_CUDA_TRY(launch_sc_complex(SC_GRAD, f64, rdA[i], call.dA[i], (int64_t)p.samples, (int)p.n, p.op, st));
+            else MGB_CUDA_TRY(launch_cplx_extract(f64, rdA[i], call.dA[i], (int64_t)p.samples, d, true, st));
         } else {
             if (!call.out || !call.out[i]) return fail(MGB_ERR_INVALID_ARGUMENT, "output buffer must not be null");
-            MGB_CUDA_TRY(launch_cplx_extract(f64, rout[i], call.out[i], (int64_t)nout, d, false, st));
-            if (rcarry[i])
-                MGB_CUDA_TRY(launch_cplx_extract(f64, rcarry[i], call.carry[i],
-                                                 (int64_t)(Q * (size_t)(p.n - 1) * (size_t)p.samples), d, false, st));
+            if (sc) MGB_CUDA_TRY(launch_sc_complex(SC_OUT, f64, rout[i], call.out[i], 0, (int)p.n, p.op, st));
+            else MGB_CUDA_TRY(launch_cplx_extract(f64, rout[i], call.out[i], (int64_t)nout, d, false, st));
+            if (rcarry[i]) {
+                if (sc) MGB_CUDA_TRY(launch_sc_complex(SC_CARRY, f64, rcarry[i], call.carry[i], (int64_t)p.samples, (int)p.n, p.op, st));
+                else MGB_CUDA_TRY(launch_cplx_extract(f64, rcarry[i], call.carry[i],
+                                                      (int64_t)(Q * (size_t)(p.n - 1) * (size_t)p.samples), d, false, st));
+            }
         }
     }
     return MGB_OK;

@@ -43,6 +43,13 @@ cudaError_t launch_small(bool fp64, int kind, int which, const InstDev* insts, i
 cudaError_t launch_cplx_embed(bool f64, const void* Z, void* out, int64_t count, int d, bool cot, cudaStream_t st);
 cudaError_t launch_cplx_extract(bool f64, const void* in, void* Z, int64_t count, int d, bool grad, cudaStream_t st);
 
+// Complex SpaceCurve data as the real 8 x 8 matrix problem (op many) on the
+// embedding of rho(0, f) (mgb_complex.cu).  count: samples (SC_EMBED,
+// SC_GRAD, SC_CARRY), unused for SC_COT / SC_OUT (n orders, op of the call).
+enum { SC_EMBED = 0, SC_COT = 1, SC_OUT = 2, SC_GRAD = 3, SC_CARRY = 4 };
+cudaError_t launch_sc_complex(int what, bool f64, const void* src, void* dst, int64_t count, int n, int op,
+                              cudaStream_t st);
+
 bool scan_tiled_ok(int kind, int d);
 cudaError_t launch_scan_tiled(const InstDev* insts, int count, int d, int nmax, const std::vector<int32_t>& active,
                               bool reverse, int f64io, cudaStream_t st);

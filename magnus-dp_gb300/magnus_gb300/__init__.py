@@ -21,10 +21,12 @@ Differences from the reference, by design:
 * ``compute_vjp(vjp_data=...)`` checks the carry's shape exactly like the
   reference and then recomputes what it needs from the chunk checkpoints
   (replaying the forward costs less than reading Q*(n-1)*S*d*d values).
-* complex64 / complex128 matrix data run as the real problem of twice the
-  dimension on [[Re A, -Im A], [Im A, Re A]] (exact: the map is an algebra
-  homomorphism); the VJP is the reference's bilinear one.  Complex
-  SpaceCurve data raise TypeError.
+* complex64 / complex128 data run on the engine's real kernels: a complex
+  d x d matrix problem as the real 2d x 2d problem on
+  [[Re A, -Im A], [Im A, Re A]], complex SpaceCurve data as the real 8 x 8
+  problem on the embedding of the quaternion right-multiplication matrix of
+  (0, f) (both maps are algebra homomorphisms, so the results are exact up to
+  rounding); the VJP is the reference's bilinear one.
 """
 from __future__ import annotations
 

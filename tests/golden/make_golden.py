@@ -146,6 +146,21 @@ def complex_cases():
                                gl_backend="serial")
             cases[f"carry_{integ}_{d}"] = dict(kind="matrix", integrator=integ, op="sum", n=4, t0=0.0, tf=1.3, A=A,
                                                out=out, carry=carry)
+    for integ, S in [("Boole", 17), ("Simpson", 13), ("Trapezoid", 11), ("Riemann", 10)]:
+        F = (rng.standard_normal((S, 3)) + 1j * rng.standard_normal((S, 3))) / 2
+        for n in (1, 2, 5):
+            for op in ("one", "many", "sum"):
+                key = f"z{idx:03d}"
+                idx += 1
+                out = core.compute_sc(n, F, 0.0, 1.3, op=op, integrator=integ, gl_backend="serial")
+                cot = rng.standard_normal(out.shape) + 1j * rng.standard_normal(out.shape)
+                dA = core.compute_sc_vjp(n, F, cot, t0=0.0, tf=1.3, op=op, integrator=integ)
+                cases[key] = dict(kind="spacecurve", integrator=integ, op=op, n=n, t0=0.0, tf=1.3, A=F, out=out,
+                                  cot=cot, dA=dA)
+        out, carry = core.compute_sc(4, F, 0.0, 1.3, op="sum", integrator=integ, gl_backend="serial",
+                                     record_vjp=True)
+        cases[f"sccarry_{integ}"] = dict(kind="spacecurve", integrator=integ, op="sum", n=4, t0=0.0, tf=1.3, A=F,
+                                         out=out, carry=carry)
     A64 = (rng.standard_normal((129, 4, 4)) + 1j * rng.standard_normal((129, 4, 4))) / 3
     A32 = A64.astype(np.complex64)
     out32 = core.compute(5, A32, 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole", gl_backend="serial")

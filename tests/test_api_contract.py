@@ -123,11 +123,13 @@ def test_divisibility_and_gl_order_errors():
         magnus.compute(130, matrix_values, 0.0, 1.0, 9)
 
 
-def test_complex_spacecurve_is_a_type_error():
-    """Complex matrix data run on the engine; complex SpaceCurve data are
-    refused at validation (before any device work)."""
-    with pytest.raises(TypeError, match="complex spacecurve"):
-        magnus.compute_sc(2, lambda t: np.ones((len(t), 3)) + 0j, 0.0, 1.0, 9)
+def test_complex_inputs_are_validated_before_device_work():
+    """Complex data take the same validation path (shape errors surface as
+    the reference's ValueError before any device work)."""
+    with pytest.raises(ValueError, match="shape"):
+        magnus.compute_sc(2, lambda t: np.ones((len(t), 4)) + 0j, 0.0, 1.0, 9)
+    with pytest.raises(ValueError, match="divisibility"):
+        magnus.compute(2, lambda t: matrix_values(t) + 0j, 0.0, 1.0, 10, integrator="Boole")
 
 
 def test_precision_keyword_is_checked():

@@ -67,3 +67,26 @@ def test_complex_autograd_matches_finite_differences(cuda):
     # for a real loss, dL = Re <conj(grad), dA> with torch's convention
     pred = (g.conj() * V).real.sum()
     assert abs(float(fd) - float(pred)) <= 1e-7 * max(1.0, abs(float(fd))), (float(fd), float(pred))
+
+
+@pytest.mark.parametrize("key", sorted(k for k in CASES if k.startswith("z")))
+def test_complex128_spacecurve_matches_reference(key, cuda):
+    c = CASES[key]
+    out = core.compute_sc(c["n"], c["A"], c["t0"], c["tf"], op=c["op"], integrator=c["integrator"],
+                          precision="plain")
+    assert out.dtype == np.complex128 and out.shape == c["out"].shape
+    assert rel(out, c["out"]) <= 1e-12, rel(out, c["out"])
+    dA = core.compute_sc_vjp(c["n"], c["A"], c["cot"], t0=c["t0"], tf=c["tf"], op=c["op"],
+                             integrator=c["integrator"], precision="plain")
+    assert dA.dtype == np.complex128 and dA.shape == c["A"].shape
+    assert rel(dA, c["dA"]) <= 1e-12, rel(dA, c["dA"])
+
+
+@pytest.mark.parametrize("key", sorted(k for k in CASES if k.startswith("sccarry")))
+def test_complex_spacecurve_carry_matches_reference(key, cuda):
+    c = CASES[key]
+    out, carry = core.compute_sc(c["n"], c["A"], c["t0"], c["tf"], op=c["op"], integrator=c["integrator"],
+                                 record_vjp=True, precision="plain")
+    assert rel(out, c["out"]) <= 1e-12
+    assert carry.shape == c["carry"].shape
+    assert rel(carry, c["carry"]) <= 1e-12, rel(carry, c["carry"])
