@@ -38,8 +38,13 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
 cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, int variant, bool prepare_only);
 int big_variants(int D);
 int big_ctas_per_sm(int D, int variant);
-// Group-tiled kernel (mgb_tuned.cu), variant 0: 2 CTAs per SM, 1: one.
+// Group-tiled kernel (mgb_tuned.cu), variant 0: 2 CTAs per SM, 1: one;
+// variant 2 (d = 32): the forward local pass on the tensor cores
+// (mgb_tiletc.cu; the VJP then takes variant 0).
 cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only);
+cudaError_t launch_tiletc(int rule, const LaunchArgs& a, int grid, bool prepare_only);
+// Device address of the time-out flag the tensor-core kernels raise.
+int* device_timeout_ptr();
 // Generic kernel variants: 8, 4 or 2 CTAs per SM.
 constexpr int GENERIC_VARIANTS = 3;
 int generic_ctas_per_sm(int variant);
