@@ -196,7 +196,7 @@ mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
 }
 
 size_t ckpt_doubles(const mgb_problem& p, const Derived& dv) { return (size_t)(2 * dv.C + 1) * dv.nm; }
-size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + (size_t)dv.Q * dv.nm + 6 * (size_t)dv.nm; }
+size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + 3 * (size_t)dv.Q * dv.nm + 6 * (size_t)dv.nm; }
 
 // Step used inside the chunk kernels (see InstDev::dt_k): the plain form
 // integrates with dt itself; the mixed form with u * 2^p, u the rule's
@@ -483,6 +483,8 @@ void plan_fill(const Call& call, PlanCore& pc, const std::vector<Derived>& dv) {
         I.eb = w; w += v.nm;
         I.db = w; w += v.nm;
         I.tt = w; w += v.nm;
+        I.dbq = w; w += (size_t)v.Q * v.nm;
+        I.tauq = w; w += (size_t)v.Q * v.nm;
         double* g = reinterpret_cast<double*>(base + pc.off_gl) + pc.gl.size();
         const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
         for (int q = 0; q < v.Q; ++q) pc.gl.push_back(gl->w[go + q]);
@@ -709,6 +711,10 @@ mgb_status seg_small(PlanCore& pc, Segment& sg, int which, int write_out, cudaSt
     const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
     if (which == SMALL_RSCAN && sg.tiled_scan)
         MGB_CUDA_TRY(timed(name, s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, true, pc.f64io, s); }));
+    else if ((which == SMALL_FIN_FWD || which == SMALL_FIN_VJP) && sg.tiled_scan)
+        MGB_CUDA_TRY(timed(name, s, [&] {
+            return launch_fin_tiled(di, sg.count, sg.d, sg.nmax, which == SMALL_FIN_VJP, write_out, pc.f64io, s);
+        }));
     else
         MGB_CUDA_TRY(timed(name, s, [&] { return launch_small(true, pc.kind, which, di, sg.count, pc.f64io, write_out, s); }));
     return MGB_OK;

@@ -60,6 +60,8 @@ struct InstDev {
     double* eb;        // n*m          : E-bar scratch
     double* db;        // n*m          : D-bar scratch
     double* tt;        // n*m          : totals T_j = sig^j * pi[C]_j
+    double* dbq;       // Q * n*m      : D-bar per node (GPU-wide adjoint)
+    double* tauq;      // Q * n*m      : tau contributions per node (GPU-wide adjoint)
     const double* glw; // Q weights on [0, 1]
     const double* glx; // Q nodes on [0, 1]
     double dt;

@@ -50,6 +50,12 @@ enum { SC_EMBED = 0, SC_COT = 1, SC_OUT = 2, SC_GRAD = 3, SC_CARRY = 4 };
 cudaError_t launch_sc_complex(int what, bool f64, const void* src, void* dst, int64_t count, int n, int op,
                               cudaStream_t st);
 
+// The small FP64 algebra after the scans, spread over the GPU (mgb_fin.cu),
+// for the same segments as the tiled scans.  vjp = false: D^(q), E, Omega
+// (and the op output when write_out); vjp = true: tau (after the former).
+cudaError_t launch_fin_tiled(const InstDev* insts, int count, int d, int nmax, bool vjp, int write_out, int f64io,
+                             cudaStream_t st);
+
 bool scan_tiled_ok(int kind, int d);
 cudaError_t launch_scan_tiled(const InstDev* insts, int count, int d, int nmax, const std::vector<int32_t>& active,
                               bool reverse, int f64io, cudaStream_t st);

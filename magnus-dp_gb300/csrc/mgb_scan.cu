@@ -13,55 +13,12 @@
 #include <vector>
 
 #include "mgb_kernels.h"
+#include "mgb_tile64.cuh"
 
 namespace mgb {
 namespace {
 
-constexpr int SNT = 256;  // 16 x 16 threads
-
-template <int T>
-struct ScanTile {
-    static constexpr int R = T / 16;  // outputs per thread along each axis
-    static constexpr int P = T + 1;   // shared-memory pitch (doubles)
-};
-
-// acc[a][b] += sum_k X[r][k] Y[k][c] over all of k, for r = r0 + ty + 16a,
-// c = c0 + tx + 16b; X is the left factor (TRANS_X: its transpose), both
-// row-major d x d.
-template <int T, bool TRANS_X>
-__device__ __forceinline__ void tile_accumulate(double (&acc)[ScanTile<T>::R][ScanTile<T>::R],
-                                                const double* __restrict__ X, const double* __restrict__ Y, int d,
-                                                int r0, int c0, double* __restrict__ sX, double* __restrict__ sY) {
-    constexpr int R = ScanTile<T>::R, P = ScanTile<T>::P;
-    const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
-    for (int k0 = 0; k0 < d; k0 += T) {
-        for (int e = tid; e < T * T; e += SNT) {
-            if (TRANS_X) {
-                const int kk = e / T, i = e % T;
-                sX[i * P + kk] = X[(int64_t)(k0 + kk) * d + r0 + i];
-            } else {
-                const int i = e / T, kk = e % T;
-                sX[i * P + kk] = X[(int64_t)(r0 + i) * d + k0 + kk];
-            }
-            const int kk = e / T, j = e % T;
-            sY[kk * P + j] = Y[(int64_t)(k0 + kk) * d + c0 + j];
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int kk = 0; kk < T; ++kk) {
-            double av[R], bv[R];
-#pragma unroll
-            for (int a = 0; a < R; ++a) av[a] = sX[(ty + 16 * a) * P + kk];
-#pragma unroll
-            for (int b = 0; b < R; ++b) bv[b] = sY[kk * P + tx + 16 * b];
-#pragma unroll
-            for (int a = 0; a < R; ++a)
-#pragma unroll
-                for (int b = 0; b < R; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
-        }
-        __syncthreads();
-    }
-}
+using namespace t64;
 
 // Block -> (instance, level j in 1..nmax, tile); levels beyond the
 // instance's order return at once (uniformly for the block).
