@@ -355,7 +355,9 @@ def run_config3(args):
                                  n=n, samples=S, dim=d, t0=0.0, tf=1.0)
         return A, cot, prob
 
-    def run_wave(idx, prec, steps):
+    picks = {}  # autotuner picks over the timed waves: "d<d> <kernel> v<variant>" -> segments
+
+    def run_wave(idx, prec, steps, record=False):
         As, cots, probs = [], [], []
         for i in idx:
             A, cot, p = make_inst(i, prec)
@@ -370,6 +372,10 @@ def run_config3(args):
             _lib.check(lib.mgb_plan_vjp(plan, s))
 
         ms = _time_graph(torch, step, steps, warmup=1)
+        if record:
+            for sg in _describe(lib, plan):
+                key = f"d{sg['d']} {sg['kernel']} v{sg['variant']}"
+                picks[key] = picks.get(key, 0) + 1
         lib.mgb_plan_destroy(plan)
         del As, dAs, outs
         torch.cuda.empty_cache()
@@ -379,13 +385,13 @@ def run_config3(args):
     for i in order:
         b = int(Ss[i]) * int(ds[i]) ** 2 * 4 * 2
         if wave and wbytes + b > wave_bytes:
-            total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1)
+            total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1, record=True)
             wave, wbytes = [], 0
         wave.append(int(i))
         wbytes += b
         total_units += int(Ss[i]) * int(ns[i])
     if wave:
-        total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1)
+        total_ms += run_wave(wave, _lib.PRECISION_MIXED, 1, record=True)
     # Mixed vs plain on the same random subsets of each dimension; both arms
     # are extrapolated to the whole batch with the same work weights, so the
     # ratio compares like with like (the measured mixed total above is the
@@ -412,7 +418,8 @@ def run_config3(args):
                       "plain_fp64_estimated": {"value": total_units / plain_est_s,
                                                "how": "4 random instances per dimension, scaled by S*n*d^2*(d+8)"},
                       "mixed_estimated": total_units / mixed_est_s,
-                      "mixed_over_plain": plain_est_s / mixed_est_s, "per_dimension_subsets": per_d}))
+                      "mixed_over_plain": plain_est_s / mixed_est_s, "per_dimension_subsets": per_d,
+                      "autotune_picks": picks}))
 
 
 # ---------------------------------------------------------------- GPU legs

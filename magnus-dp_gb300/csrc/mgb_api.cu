@@ -365,7 +365,11 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     // segments: runs of equal dimension
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    const size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 2, (size_t)48 << 30));
+    size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 2, (size_t)48 << 30));
+    // MGB_SCRATCH_MB: a fixed scratch budget in MiB (tests use it to make the
+    // segments' slot counts shrink below their asks)
+    if (const char* ev = std::getenv("MGB_SCRATCH_MB"))
+        if (std::atoll(ev) > 0) budget = (size_t)std::atoll(ev) << 20;
     int64_t wpos = 0;
     for (size_t a = 0; a < call.count;) {
         size_t b = a;

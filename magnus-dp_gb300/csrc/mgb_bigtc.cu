@@ -49,18 +49,20 @@ namespace {
 
 constexpr int TNT = 256;
 
-// KB: k-block per stage (32 or 64; the autotuner picks)
-template <int D, int KB>
+// KB: k-block per stage (32 or 64); NACC: accumulator pairs (2: the
+// epilogue of one sample overlaps the MMAs of the next; 1: half the tensor
+// memory, so that two d = 128 CTAs share an SM).  The autotuner picks.
+template <int D, int KB, int NACC = 2>
 struct TcCfg {
     static constexpr int m = D * D;
     static constexpr uint32_t TILE = D * KB * 2;              // bytes per operand piece (bf16)
     static constexpr uint32_t STAGE = 6 * TILE;               // X0 X1 X2 Y0 Y1 Y2
     static constexpr uint32_t LBO = D * 16, SBO = 128;        // bytes
-    static constexpr uint32_t NCOL = 4 * D;                   // two samples x (main, small) accumulators
-    // D = 128 takes 4 x 128 columns, all of an SM's tensor memory: its shared
-    // memory request is padded so that no other CTA of these kernels fits on
-    // the SM beside it.
-    static constexpr size_t SMEM = D == 128 ? (size_t)200 * 1024 : 2 * (size_t)STAGE + 64;
+    static constexpr uint32_t NCOL = 2 * NACC * D;            // NACC samples x (main, small) accumulators
+    // D = 128 with two accumulator pairs takes 4 x 128 columns, all of an
+    // SM's tensor memory: its shared memory request is padded so that no
+    // other CTA of these kernels fits on the SM beside it.
+    static constexpr size_t SMEM = (D == 128 && NACC == 2) ? (size_t)200 * 1024 : 2 * (size_t)STAGE + 64;
     static constexpr size_t BAR_OFF = 2 * (size_t)STAGE;
     static constexpr int NKB = D / KB;
     // kind::f16 instruction descriptor: F32 accumulator (bits 4-5 = 1), BF16 A
@@ -138,17 +140,18 @@ __device__ __forceinline__ void store_tile(uint8_t* t, const TileRegs<D, KB>& r)
 struct Pipe {
     uint32_t kt, ns;         // stages and samples issued so far (uniform)
     uint32_t tbase;          // tensor memory base
-    uint32_t mb;             // mbarriers: [0,1] stages, [2,3] accumulators, [4] final
+    uint32_t mb;             // mbarriers: [0,1] stages, [2,3] accumulators (NACC = 1: [2]), [4] final
     uint8_t* stg;            // two stages
     bool ok;                 // this thread saw no time-out
 };
 
-// Accumulator `a` of sample counter s -> out (row-major D x D), stored or added.
-template <int D>
+// Accumulator of sample counter s -> out (row-major D x D), stored or added.
+template <int D, int NACC>
 __device__ __forceinline__ void epilogue(Pipe& pp, uint32_t s, float* __restrict__ out, bool add) {
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, q = warp & 3, h = warp >> 2;
-    const uint32_t a = s & 1;
-    if (pp.ok && !mbar_wait(pp.mb + 8 * (2 + a), (s >> 1) & 1)) pp.ok = false;
+    const uint32_t a = NACC == 2 ? (s & 1) : 0u;
+    const uint32_t par = NACC == 2 ? ((s >> 1) & 1) : (s & 1);
+    if (pp.ok && !mbar_wait(pp.mb + 8 * (2 + a), par)) pp.ok = false;
     pp.ok = __all_sync(0xffffffffu, pp.ok);  // tcgen05.ld is warp-collective
     fence_after();
     if (!pp.ok) return;
@@ -184,10 +187,10 @@ __device__ __forceinline__ void epilogue(Pipe& pp, uint32_t s, float* __restrict
 // D*D per sample.  XT / YT: the operand's K-major tile is the transpose of
 // the stored matrix (X: element (r, k) = X[k][r]; Y: B^T element (n, k) =
 // Y[k][n] for YT, Y[n][k] otherwise).  Returns false on a time-out (uniform).
-template <int D, int KB, bool XT, bool YT>
+template <int D, int KB, int NACC, bool XT, bool YT>
 __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __restrict__ Y, float* __restrict__ out,
                         bool add, int l0, int l1) {
-    using Cf = TcCfg<D, KB>;
+    using Cf = TcCfg<D, KB, NACC>;
     constexpr int m = Cf::m;
     const int cnt = l1 - l0 + 1;
     if (cnt <= 0) return true;
@@ -197,8 +200,12 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
     for (int idx = 0; idx <= cnt; ++idx) {
         if (idx < cnt) {
             const int li = l0 + idx;
-            const uint32_t a = pp.ns & 1;
+            const uint32_t a = NACC == 2 ? (pp.ns & 1) : 0u;
             for (int kb = 0; kb < Cf::NKB; ++kb) {
+                // one accumulator pair: the previous sample's epilogue frees
+                // it before this sample's first MMA (the barrier below orders
+                // its tensor-memory loads before the issue)
+                if (NACC == 1 && kb == 0 && idx > 0) epilogue<D, NACC>(pp, pp.ns - 1, out + (int64_t)(li - 1) * m, add);
                 const uint32_t b = pp.kt & 1;
                 if (pp.kt >= 2 && pp.ok && !mbar_wait(pp.mb + 8 * b, ((pp.kt - 2) >> 1) & 1)) pp.ok = false;
                 uint8_t* xs = pp.stg + (size_t)b * Cf::STAGE;
@@ -241,11 +248,11 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
                     load_tile<D, KB, XT>(rx, X + (int64_t)nli * m, nkb);
                     load_tile<D, KB, YT>(ry, Y + (int64_t)nli * m, nkb);
                 }
-                if (kb == 0 && idx > 0) epilogue<D>(pp, pp.ns - 1, out + (int64_t)(li - 1) * m, add);
+                if (NACC == 2 && kb == 0 && idx > 0) epilogue<D, NACC>(pp, pp.ns - 1, out + (int64_t)(li - 1) * m, add);
             }
             ++pp.ns;
         } else {
-            epilogue<D>(pp, pp.ns - 1, out + (int64_t)(l1)*m, add);
+            epilogue<D, NACC>(pp, pp.ns - 1, out + (int64_t)(l1)*m, add);
         }
     }
     return !__syncthreads_or(!pp.ok);
@@ -354,11 +361,11 @@ __device__ __forceinline__ void prefix_rev(const float* __restrict__ H, float* _
 }
 
 // ------------------------------------------------------------ the kernel
-template <int D, int KB, int RULE, int MODE, int MINB>
+template <int D, int KB, int RULE, int MODE, int MINB, int NACC>
 __global__ void __launch_bounds__(TNT, MINB)
     k_bigtc(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work, int64_t nwork,
             float* __restrict__ scratch, int64_t slot_elems) {
-    using Cf = TcCfg<D, KB>;
+    using Cf = TcCfg<D, KB, NACC>;
     constexpr int m = Cf::m;
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cf::BAR_OFF);
@@ -417,7 +424,7 @@ __global__ void __launch_bounds__(TNT, MINB)
             prefix_fwd<RULE>(F, Pj, keep, carry, lam, m, Kp, first, riem0, kc);
             __syncthreads();
             if (j < NL) {
-                alive = tc_pass<D, KB, false, true>(pp, Ag, Pj, Wb, false, 0, Kp);  // W = A P
+                alive = tc_pass<D, KB, NACC, false, true>(pp, Ag, Pj, Wb, false, 0, Kp);  // W = A P
                 F = Wb;
             }
         }
@@ -427,8 +434,8 @@ __global__ void __launch_bounds__(TNT, MINB)
             for (int j = n; j >= 1 && alive; --j) {
                 if (j < n) {
                     const float* Pj = tape + (int64_t)(j - 1) * Lm;
-                    alive = tc_pass<D, KB, true, true>(pp, Ag, Gb, Hb, false, first, Kp);         // H = A^T G
-                    if (alive) alive = tc_pass<D, KB, false, false>(pp, Gb, Pj, dAb, j < n - 1, 0, Kp);  // dA += G P^T
+                    alive = tc_pass<D, KB, NACC, true, true>(pp, Ag, Gb, Hb, false, first, Kp);         // H = A^T G
+                    if (alive) alive = tc_pass<D, KB, NACC, false, false>(pp, Gb, Pj, dAb, j < n - 1, 0, Kp);  // dA += G P^T
                     if (!alive) break;
                 }
                 prefix_rev<RULE>(j < n ? Hb : nullptr, Gb, rc + (int64_t)(j - 1) * m, m, Kp, first, riem0, kc);
@@ -474,7 +481,7 @@ __global__ void __launch_bounds__(TNT, MINB)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(pp.tbase), "r"(Cf::NCOL) : "memory");
 }
 
-template <int D, int KB, int RULE, int MODE, int MINB>
+template <int D, int KB, int RULE, int MODE, int MINB, int NACC>
 cudaError_t set_attr() {
     static std::mutex mu;
     static std::vector<bool> done;
@@ -484,50 +491,54 @@ cudaError_t set_attr() {
     std::lock_guard<std::mutex> lock(mu);
     if ((int)done.size() <= dev) done.resize(dev + 1, false);
     if (done[dev]) return cudaSuccess;
-    e = cudaFuncSetAttribute(k_bigtc<D, KB, RULE, MODE, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)TcCfg<D, KB>::SMEM);
+    e = cudaFuncSetAttribute(k_bigtc<D, KB, RULE, MODE, MINB, NACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)TcCfg<D, KB, NACC>::SMEM);
     if (e == cudaSuccess) done[dev] = true;
     return e;
 }
 
-template <int D, int KB, int RULE, int MODE, int MINB>
+template <int D, int KB, int RULE, int MODE, int MINB, int NACC>
 cudaError_t launch_t(const LaunchArgs& a, int grid, bool prepare_only) {
-    cudaError_t e = set_attr<D, KB, RULE, MODE, MINB>();
+    cudaError_t e = set_attr<D, KB, RULE, MODE, MINB, NACC>();
     if (e != cudaSuccess || prepare_only) return e;
-    k_bigtc<D, KB, RULE, MODE, MINB><<<grid, TNT, TcCfg<D, KB>::SMEM, a.stream>>>(
+    k_bigtc<D, KB, RULE, MODE, MINB, NACC><<<grid, TNT, TcCfg<D, KB, NACC>::SMEM, a.stream>>>(
         a.insts, a.work, a.nwork, static_cast<float*>(a.scratch), a.slot_elems);
     return cudaGetLastError();
 }
 
-template <int D, int KB, int MODE, int MINB>
+template <int D, int KB, int MODE, int MINB, int NACC>
 cudaError_t launch_r(int rule, const LaunchArgs& a, int grid, bool prepare_only) {
     switch (rule) {
-        case R_BOOLE: return launch_t<D, KB, R_BOOLE, MODE, MINB>(a, grid, prepare_only);
-        case R_SIMPSON: return launch_t<D, KB, R_SIMPSON, MODE, MINB>(a, grid, prepare_only);
-        case R_TRAP: return launch_t<D, KB, R_TRAP, MODE, MINB>(a, grid, prepare_only);
-        default: return launch_t<D, KB, R_RIEMANN, MODE, MINB>(a, grid, prepare_only);
+        case R_BOOLE: return launch_t<D, KB, R_BOOLE, MODE, MINB, NACC>(a, grid, prepare_only);
+        case R_SIMPSON: return launch_t<D, KB, R_SIMPSON, MODE, MINB, NACC>(a, grid, prepare_only);
+        case R_TRAP: return launch_t<D, KB, R_TRAP, MODE, MINB, NACC>(a, grid, prepare_only);
+        default: return launch_t<D, KB, R_RIEMANN, MODE, MINB, NACC>(a, grid, prepare_only);
     }
 }
 
-template <int D, int KB, int MINB>
+template <int D, int KB, int MINB, int NACC = 2>
 cudaError_t launch_m(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only) {
-    return mode == MODE_LOCAL ? launch_r<D, KB, MODE_LOCAL, MINB>(rule, a, grid, prepare_only)
-                              : launch_r<D, KB, MODE_VJP, MINB>(rule, a, grid, prepare_only);
+    return mode == MODE_LOCAL ? launch_r<D, KB, MODE_LOCAL, MINB, NACC>(rule, a, grid, prepare_only)
+                              : launch_r<D, KB, MODE_VJP, MINB, NACC>(rule, a, grid, prepare_only);
 }
 
 }  // namespace
 
-int big_variants(int D) { return D == 64 ? 4 : 2; }
-int big_ctas_per_sm(int D, int variant) { return (D == 64 && variant < 2) ? 2 : 1; }
+int big_variants(int D) { return D == 64 ? 4 : 3; }
+int big_ctas_per_sm(int D, int variant) { return ((D == 64 && variant < 2) || (D == 128 && variant == 2)) ? 2 : 1; }
 
 // variant: D = 64: 0 KB 32 / 2 CTAs per SM, 1 KB 64 / 2, 2 KB 32 / 1, 3 KB 64 / 1;
-//          D = 128: 0 KB 32, 1 KB 64 (one CTA per SM).
+//          D = 128: 0 KB 32, 1 KB 64 (one CTA per SM, two accumulator pairs),
+//          2 KB 32 with one accumulator pair, two CTAs per SM.
 cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, int variant, bool prepare_only) {
     const int ctas = sms * big_ctas_per_sm(D, variant);
     int grid = (int)std::min<int64_t>(a.grid, (int64_t)ctas);
     if (grid < 1) grid = 1;
-    if (D == 128) return variant == 1 ? launch_m<128, 64, 1>(rule, mode, a, grid, prepare_only)
-                                      : launch_m<128, 32, 1>(rule, mode, a, grid, prepare_only);
+    if (D == 128) {
+        if (variant == 2) return launch_m<128, 32, 2, 1>(rule, mode, a, grid, prepare_only);
+        return variant == 1 ? launch_m<128, 64, 1>(rule, mode, a, grid, prepare_only)
+                            : launch_m<128, 32, 1>(rule, mode, a, grid, prepare_only);
+    }
     switch (variant) {
         case 1: return launch_m<64, 64, 2>(rule, mode, a, grid, prepare_only);
         case 2: return launch_m<64, 32, 1>(rule, mode, a, grid, prepare_only);

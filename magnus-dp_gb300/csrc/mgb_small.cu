@@ -111,15 +111,19 @@ __device__ __forceinline__ void write_dA(const InstDev& I, int64_t i, const T* v
 
 template <class T, int KIND, int RULE, int MODE>
 __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts, const ChunkRef* __restrict__ work,
-                                               int64_t nwork, T* __restrict__ scratch, int64_t slot_elems, int f64io) {
+                                               int64_t nwork, T* __restrict__ scratch, int64_t slot_elems, int64_t nslots,
+                                               int f64io) {
     using Al = Small<T, KIND>;
     constexpr int BS = Block<RULE>::BS;
     const bool f64 = f64io != 0;
+    // one tape slot per working thread: the last block's threads beyond the
+    // slot count (the scratch budget need not be a multiple of the block
+    // size) take no work
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    if (tid >= nslots) return;
     T* const tape = scratch + tid * slot_elems;  // [L][NMAX-1][4] prefix values P_j
 
-    for (int64_t w = tid; w < nwork; w += nthreads) {
+    for (int64_t w = tid; w < nwork; w += nslots) {
         const ChunkRef wk = work[w];
         const InstDev& I = insts[wk.inst];
         const int c = wk.chunk, n = I.n;
@@ -290,10 +294,10 @@ cudaError_t launch_small_t(int mode, const LaunchArgs& a, int64_t threads) {
     T* scr = static_cast<T*>(a.scratch);
     if (mode == MODE_LOCAL)
         k_small<T, KIND, RULE, MODE_LOCAL><<<blocks, SNT, 0, a.stream>>>(a.insts, a.work, a.nwork, scr,
-                                                                          a.slot_elems, a.f64io);
+                                                                          a.slot_elems, threads, a.f64io);
     else
         k_small<T, KIND, RULE, MODE_VJP><<<blocks, SNT, 0, a.stream>>>(a.insts, a.work, a.nwork, scr,
-                                                                        a.slot_elems, a.f64io);
+                                                                        a.slot_elems, threads, a.f64io);
     return cudaGetLastError();
 }
 

@@ -46,7 +46,10 @@ constexpr uint32_t NCOL = 256;                  // accumulators: main (128 colum
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr size_t OFF_X = 0, OFF_Y = 3 * TILE, OFF_F = 6 * TILE;
 constexpr size_t OFF_BAR = OFF_F + (size_t)G * D * PF * sizeof(float);
-constexpr size_t SMEM = OFF_BAR + 64;
+// Padded so that at most two CTAs fit on an SM whatever the register count:
+// two take all of its tensor memory, and a third would wait in
+// tcgen05.alloc until one of them finished its whole work list.
+constexpr size_t SMEM = (OFF_BAR + 64) > 80 * 1024 ? OFF_BAR + 64 : 80 * 1024;
 
 // byte offset of element (row r, column k) of a 128 x 32 K-major BF16 tile
 __device__ __forceinline__ uint32_t off128(int r, int k) {
@@ -137,10 +140,12 @@ __global__ void __launch_bounds__(TT, 2)
             }
             __syncthreads();
 
-            for (int j = 1; j <= n; ++j) {
-                // ---- prefix pass of level j over the group's samples
-                float* sj = st + (j - 1) * 3 * m;
-                FwdState<float> fs[4];
+            // prefix state of a level (this thread's elements; it alone
+            // reads and writes them), loaded one level ahead: level j + 1's
+            // loads are in flight while level j's MMAs run
+            FwdState<float> fs[4];
+            auto load_state = [&](int j) {
+                const float* sj = st + (j - 1) * 3 * m;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int el = (4 * pig + q) * D + pc;
@@ -149,6 +154,11 @@ __global__ void __launch_bounds__(TT, 2)
                     fs[q].f0 = sj[2 * m + el];
                     fs[q].f1 = fs[q].f2 = fs[q].f3 = 0.f;
                 }
+            };
+            load_state(1);
+            for (int j = 1; j <= n; ++j) {
+                // ---- prefix pass of level j over the group's samples
+                float* sj = st + (j - 1) * 3 * m;
                 const Carry<float> zc{0.f, 0.f};
                 float P[G][4];
 #pragma unroll
@@ -199,6 +209,7 @@ __global__ void __launch_bounds__(TT, 2)
                     }
                     mma_commit(su32(bar));
                 }
+                load_state(j + 1);
                 bool ok = mbar_wait(su32(bar), uses & 1);
                 ++uses;
                 ok = __all_sync(0xffffffffu, ok);

@@ -561,8 +561,11 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
         sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4;  // one thread's tape
         want = std::min<int64_t>(nwork, (int64_t)sms * 1024);
     } else if (tc.use) {
+        int cps = tc.ctas_per_sm;
+        if (tc.family == 3)
+            for (int v = 0; v < tc.nvariants; ++v) cps = std::max(cps, big_ctas_per_sm(tc.D, v));
         sz.slot_elems = generic;
-        want = std::min<int64_t>(nwork, (int64_t)sms * tc.ctas_per_sm);
+        want = std::min<int64_t>(nwork, (int64_t)sms * cps);
     } else {
         sz.slot_elems = generic;
         want = std::min<int64_t>(nwork, (int64_t)sms * 8);

@@ -60,7 +60,7 @@ RULES = {0: "Boole", 1: "Simpson", 2: "Trapezoid", 3: "Riemann"}
     (32, 3, _lib.PRECISION_MIXED, "float32", 1e-6, "k_tile"),  # 2: tensor-core forward
     (16, 2, _lib.PRECISION_MIXED, "float32", 1e-6, "k_tile"),
     (64, 4, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),
-    (128, 2, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),
+    (128, 3, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),  # 2: one accumulator pair, 2 CTAs/SM
     (8, 3, _lib.PRECISION_PLAIN, "float64", 1e-12, "k_chunk"),
 ])
 @pytest.mark.parametrize("integrator", [0, 1])
@@ -101,3 +101,21 @@ def test_autotune_off_keeps_variant_zero(cuda, monkeypatch):
     _, _, _, desc = _run_plan(cuda, [(16, 257, 4)], _lib.PRECISION_MIXED, "float32")
     seg = desc["segments"][0]
     assert seg["variant"] == 0 and seg["tuned_ms"] == []
+
+
+@pytest.mark.parametrize("precision,dtype_name,tol", [(_lib.PRECISION_MIXED, "float32", 1e-6),
+                                                      (_lib.PRECISION_PLAIN, "float64", 1e-12)])
+def test_scratch_cut_keeps_results(precision, dtype_name, tol, cuda, monkeypatch):
+    """A scratch budget below the segments' asks shrinks every segment's slot
+    count in the same proportion; the thread-per-chunk kernel (d = 2) then
+    runs with a slot count that is not a multiple of its block size, and its
+    last block's spare threads must stay off the scratch."""
+    monkeypatch.setenv("MGB_SCRATCH_MB", "1")
+    specs = [(2, 4097, 4)] * 6 + [(64, 257, 4)]
+    host, outs, dAs, desc = _run_plan(cuda, specs, precision, dtype_name, K=8)
+    seg = next(s for s in desc["segments"] if s["d"] == 2)
+    assert seg["slots"] < seg["chunks"] and seg["slots"] % 128 != 0, seg
+    for (A, cot, n), o, g in zip(host, outs, dAs):
+        A64 = A.astype(np.float64)
+        assert rel(o, O.forward(A64, n, 0.0, 1.0, "sum", "Boole")) <= tol
+        assert rel(g, O.vjp(A64, cot.astype(np.float64), n, 0.0, 1.0, "sum", "Boole")) <= tol
