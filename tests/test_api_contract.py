@@ -135,3 +135,31 @@ def test_complex_inputs_are_validated_before_device_work():
 def test_precision_keyword_is_checked():
     with pytest.raises(ValueError, match="precision"):
         magnus.compute(1, matrix_values, 0.0, 1.0, 9, precision="bf16")
+
+
+def test_generated_typing_matches_the_name_lists():
+    """The committed Literal aliases are what the generator writes from the
+    package's dispatch-name lists (src/api/typing_gen.cpp:43-50 in the
+    reference), and each alias lists exactly the metadata function's names."""
+    import inspect
+    import typing
+
+    from magnus_gb300 import _generated_typing as gt
+    from magnus_gb300 import _typing_gen
+    assert inspect.getsource(gt) == _typing_gen.typing_source()
+    assert typing.get_args(gt.MatrixBackendName) == magnus.matrix_backends()
+    assert typing.get_args(gt.IntegratorName) == magnus.integrators()
+    assert typing.get_args(gt.GLBackendName) == magnus.gl_backends()
+    assert typing.get_args(gt.NumericBackendName) == magnus.numeric_backends()
+    assert typing.get_args(gt.KernelOpName) == magnus.ops()
+
+
+def test_stub_declares_every_public_name():
+    import ast
+    import os
+    stub = os.path.join(os.path.dirname(magnus.__file__), "__init__.pyi")
+    with open(stub, encoding="utf-8") as f:
+        tree = ast.parse(f.read())
+    declared = {node.name for node in tree.body if isinstance(node, ast.FunctionDef)}
+    assert set(magnus.__all__) <= declared
+    assert os.path.exists(os.path.join(os.path.dirname(magnus.__file__), "py.typed"))
