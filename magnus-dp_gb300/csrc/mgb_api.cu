@@ -701,13 +701,16 @@ mgb_status seg_chunks(PlanCore& pc, Segment& sg, int mode, cudaStream_t s, const
     return MGB_OK;
 }
 
+// Largest n d^2 of a segment's instances (SpaceCurves: d = 2, 4-vectors).
+int64_t seg_nm(const Segment& sg) { return (int64_t)sg.nmax * sg.d * sg.d; }
+
 // Forward scan over a segment's chunks: pi^0..pi^C.
 mgb_status seg_scan(PlanCore& pc, Segment& sg, cudaStream_t s) {
     const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
     if (sg.tiled_scan)
         MGB_CUDA_TRY(timed("scan", s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, false, pc.f64io, s); }));
     else
-        MGB_CUDA_TRY(timed("scan", s, [&] { return launch_small(true, pc.kind, SMALL_SCAN, di, sg.count, pc.f64io, 0, s); }));
+        MGB_CUDA_TRY(timed("scan", s, [&] { return launch_small(true, pc.kind, SMALL_SCAN, di, sg.count, pc.f64io, 0, seg_nm(sg), s); }));
     return MGB_OK;
 }
 
@@ -720,7 +723,7 @@ mgb_status seg_small(PlanCore& pc, Segment& sg, int which, int write_out, cudaSt
             return launch_fin_tiled(di, sg.count, sg.d, sg.nmax, which == SMALL_FIN_VJP, write_out, pc.f64io, s);
         }));
     else
-        MGB_CUDA_TRY(timed(name, s, [&] { return launch_small(true, pc.kind, which, di, sg.count, pc.f64io, write_out, s); }));
+        MGB_CUDA_TRY(timed(name, s, [&] { return launch_small(true, pc.kind, which, di, sg.count, pc.f64io, write_out, seg_nm(sg), s); }));
     return MGB_OK;
 }
 
@@ -1609,7 +1612,7 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
     la.stream = cs;
     const std::vector<InstDev> hi(1, I);
     MGB_CUDA_TRY(launch_chunk_any(plain, p->kind, p->integrator, MODE_LOCAL, la, hi, di.sms, 0));
-    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_SCAN, d_inst, 1, f64io, 0, cs));
-    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_FIN_FWD, d_inst, 1, f64io, 1, cs));
+    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_SCAN, d_inst, 1, f64io, 0, (int64_t)p->n * v.m, cs));
+    MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_FIN_FWD, d_inst, 1, f64io, 1, (int64_t)p->n * v.m, cs));
     return MGB_OK;
 }

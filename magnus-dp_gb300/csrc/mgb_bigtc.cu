@@ -259,7 +259,8 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
 }
 
 // ------------------------------------------------------------ prefix passes
-constexpr int PF = 8;  // samples of loads in flight per thread
+// PF: samples of loads in flight per thread (8; 4 in the three-CTA variant,
+// whose register budget is smaller)
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
@@ -267,7 +268,7 @@ __device__ __forceinline__ float comp(const float4& v, int u) { return u == 0 ? 
 
 // P_j over the chunk from f (F) for levels with a carry row pic_j (nullptr:
 // zero); keep: write P to the tape; lam_j (MODE_LOCAL): the chunk total.
-template <int RULE>
+template <int RULE, int PF, bool CY>
 __device__ __forceinline__ void prefix_fwd(const float* __restrict__ F, float* __restrict__ Pj, bool keep,
                                            const double* __restrict__ pic_j, double* __restrict__ lam_j, int m, int Kp,
                                            int first, bool riem0, const RuleCoef<float>& kc) {
@@ -302,10 +303,10 @@ __device__ __forceinline__ void prefix_fwd(const float* __restrict__ F, float* _
                 const int li = l0 + u;
                 if (li <= Kp) {
                     float4 P;
-                    P.x = fwd_step<float, RULE>(s[0], cur[u].x, li, kc, cy[0]);
-                    P.y = fwd_step<float, RULE>(s[1], cur[u].y, li, kc, cy[1]);
-                    P.z = fwd_step<float, RULE>(s[2], cur[u].z, li, kc, cy[2]);
-                    P.w = fwd_step<float, RULE>(s[3], cur[u].w, li, kc, cy[3]);
+                    P.x = fwd_step<float, RULE, CY>(s[0], cur[u].x, li, kc, cy[0]);
+                    P.y = fwd_step<float, RULE, CY>(s[1], cur[u].y, li, kc, cy[1]);
+                    P.z = fwd_step<float, RULE, CY>(s[2], cur[u].z, li, kc, cy[2]);
+                    P.w = fwd_step<float, RULE, CY>(s[3], cur[u].w, li, kc, cy[3]);
                     if (keep) st4(Pj + (int64_t)li * m + e4, P);
                 }
             }
@@ -318,7 +319,7 @@ __device__ __forceinline__ void prefix_fwd(const float* __restrict__ F, float* _
 
 // G over the chunk (positions Kp..first) from H (nullptr: zero) and the
 // carry row rc_j; G[0] = pend unless riem0.
-template <int RULE>
+template <int RULE, int PF>
 __device__ __forceinline__ void prefix_rev(const float* __restrict__ H, float* __restrict__ G,
                                            const double* __restrict__ rc_j, int m, int Kp, int first, bool riem0,
                                            const RuleCoef<float>& kc) {
@@ -367,6 +368,7 @@ __global__ void __launch_bounds__(TNT, MINB)
             float* __restrict__ scratch, int64_t slot_elems) {
     using Cf = TcCfg<D, KB, NACC>;
     constexpr int m = Cf::m;
+    constexpr int PF = MINB >= 3 ? 4 : 8;
     extern __shared__ __align__(1024) uint8_t smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Cf::BAR_OFF);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(TNT, MINB)
             float* Pj = tape + (int64_t)((j < n ? j : 1) - 1) * Lm;
             const double* carry = (MODE == MODE_LOCAL || riem0) ? nullptr : pic + (int64_t)(j - 1) * m;
             double* lam = (MODE == MODE_LOCAL) ? I.lam + (int64_t)c * nm + (int64_t)(j - 1) * m : nullptr;
-            prefix_fwd<RULE>(F, Pj, keep, carry, lam, m, Kp, first, riem0, kc);
+            prefix_fwd<RULE, PF, MODE != MODE_LOCAL>(F, Pj, keep, carry, lam, m, Kp, first, riem0, kc);
             __syncthreads();
             if (j < NL) {
                 alive = tc_pass<D, KB, NACC, false, true>(pp, Ag, Pj, Wb, false, 0, Kp);  // W = A P
@@ -438,7 +440,7 @@ __global__ void __launch_bounds__(TNT, MINB)
                     if (alive) alive = tc_pass<D, KB, NACC, false, false>(pp, Gb, Pj, dAb, j < n - 1, 0, Kp);  // dA += G P^T
                     if (!alive) break;
                 }
-                prefix_rev<RULE>(j < n ? Hb : nullptr, Gb, rc + (int64_t)(j - 1) * m, m, Kp, first, riem0, kc);
+                prefix_rev<RULE, PF>(j < n ? Hb : nullptr, Gb, rc + (int64_t)(j - 1) * m, m, Kp, first, riem0, kc);
                 __syncthreads();
             }
             if (alive) {
@@ -524,10 +526,14 @@ cudaError_t launch_m(int rule, int mode, const LaunchArgs& a, int grid, bool pre
 
 }  // namespace
 
-int big_variants(int D) { return D == 64 ? 4 : 3; }
-int big_ctas_per_sm(int D, int variant) { return ((D == 64 && variant < 2) || (D == 128 && variant == 2)) ? 2 : 1; }
+int big_variants(int D) { return D == 64 ? 5 : 3; }
+int big_ctas_per_sm(int D, int variant) {
+    if (D == 64) return variant == 4 ? 3 : (variant < 2 ? 2 : 1);
+    return variant == 2 ? 2 : 1;
+}
 
-// variant: D = 64: 0 KB 32 / 2 CTAs per SM, 1 KB 64 / 2, 2 KB 32 / 1, 3 KB 64 / 1;
+// variant: D = 64: 0 KB 32 / 2 CTAs per SM, 1 KB 64 / 2, 2 KB 32 / 1, 3 KB 64 / 1,
+//                  4 KB 32 with one accumulator pair / 3;
 //          D = 128: 0 KB 32, 1 KB 64 (one CTA per SM, two accumulator pairs),
 //          2 KB 32 with one accumulator pair, two CTAs per SM.
 cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, int variant, bool prepare_only) {
@@ -543,6 +549,7 @@ cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, 
         case 1: return launch_m<64, 64, 2>(rule, mode, a, grid, prepare_only);
         case 2: return launch_m<64, 32, 1>(rule, mode, a, grid, prepare_only);
         case 3: return launch_m<64, 64, 1>(rule, mode, a, grid, prepare_only);
+        case 4: return launch_m<64, 32, 3, 1>(rule, mode, a, grid, prepare_only);
         default: return launch_m<64, 32, 2>(rule, mode, a, grid, prepare_only);
     }
 }

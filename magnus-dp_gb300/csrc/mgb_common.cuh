@@ -145,42 +145,38 @@ struct Alg<T, KIND_MATRIX> {
     }
 };
 
-// qmul(a, b) = b (x) a (Hamilton).
+// qmul(a, b) = b (x) a (Hamilton).  Component el of each product is
+// sum_k sign(el, k) x[k] y[el ^ k]; the signs are bit masks (bit 4 el + k
+// set: negative), so that the lanes of a warp holding different components
+// run the same instructions (a switch on el diverged four ways).
+//   mul  (a, b): sum_k +-b[k] a[el ^ k]
+//   adjL (a, g): sum_k +-g[k] a[el ^ k]
+//   adjR (g, b): sum_k +-g[k] b[el ^ k]
 template <class T>
 struct Alg<T, KIND_SC> {
+    static constexpr unsigned kMul = 0x428Eu, kAdjL = 0x3950u, kAdjR = 0x5390u;
+    template <class PX, class PY>
+    __device__ __forceinline__ static T signed_sum(unsigned mask, const PX* x, const PY* y, int el) {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const T t = (T)x[k] * (T)y[el ^ k];
+            s += ((mask >> (4 * el + k)) & 1u) ? -t : t;
+        }
+        return s;
+    }
     __device__ __forceinline__ static T one(int, int el) { return el == 0 ? T(1) : T(0); }
     template <class PA, class PB>
     __device__ __forceinline__ static T mul(const PA* pa, const PB* pb, int, int el) {
-        const T a0 = (T)pa[0], a1 = (T)pa[1], a2 = (T)pa[2], a3 = (T)pa[3];
-        const T b0 = (T)pb[0], b1 = (T)pb[1], b2 = (T)pb[2], b3 = (T)pb[3];
-        switch (el) {
-            case 0: return b0 * a0 - b1 * a1 - b2 * a2 - b3 * a3;
-            case 1: return b0 * a1 + b1 * a0 + b2 * a3 - b3 * a2;
-            case 2: return b0 * a2 - b1 * a3 + b2 * a0 + b3 * a1;
-            default: return b0 * a3 + b1 * a2 - b2 * a1 + b3 * a0;
-        }
+        return signed_sum(kMul, pb, pa, el);
     }
     template <class PA, class PB>
     __device__ __forceinline__ static T adjL(const PA* pa, const PB* pg, int, int el) {
-        const T a0 = (T)pa[0], a1 = (T)pa[1], a2 = (T)pa[2], a3 = (T)pa[3];
-        const T g0 = (T)pg[0], g1 = (T)pg[1], g2 = (T)pg[2], g3 = (T)pg[3];
-        switch (el) {
-            case 0: return a0 * g0 + a1 * g1 + a2 * g2 + a3 * g3;
-            case 1: return -a1 * g0 + a0 * g1 - a3 * g2 + a2 * g3;
-            case 2: return -a2 * g0 + a3 * g1 + a0 * g2 - a1 * g3;
-            default: return -a3 * g0 - a2 * g1 + a1 * g2 + a0 * g3;
-        }
+        return signed_sum(kAdjL, pg, pa, el);
     }
     template <class PA, class PB>
     __device__ __forceinline__ static T adjR(const PA* pg, const PB* pb, int, int el) {
-        const T p0 = (T)pb[0], p1 = (T)pb[1], p2 = (T)pb[2], p3 = (T)pb[3];
-        const T g0 = (T)pg[0], g1 = (T)pg[1], g2 = (T)pg[2], g3 = (T)pg[3];
-        switch (el) {
-            case 0: return p0 * g0 + p1 * g1 + p2 * g2 + p3 * g3;
-            case 1: return -p1 * g0 + p0 * g1 + p3 * g2 - p2 * g3;
-            case 2: return -p2 * g0 - p3 * g1 + p0 * g2 + p1 * g3;
-            default: return -p3 * g0 + p2 * g1 - p1 * g2 + p0 * g3;
-        }
+        return signed_sum(kAdjR, pg, pb, el);
     }
 };
 
@@ -255,8 +251,10 @@ struct FwdState {
 };
 
 // Returns P at position li (carry included) given f at li; updates the state.
-template <class T, int RULE>
+// CY = false: the caller's carry is zero (local passes), P is the local value.
+template <class T, int RULE, bool CY = true>
 __device__ __forceinline__ T fwd_step(FwdState<T>& s, T f, int li, const RuleCoef<T>& k, const Carry<T>& cy) {
+    auto add_carry = [&](T local, const Carry<T>& c) { return CY ? mgb::add_carry(local, c) : local; };
     if (RULE == R_BOOLE) {
         switch (li & 3) {
             case 1: s.f1 = f; return add_carry((f * k.h + s.f0 * k.h + s.blo) + s.base, cy);

@@ -27,9 +27,11 @@ struct LaunchArgs {
 // elements: (n + 4) * (K + 1) * m for the largest instance.
 cudaError_t launch_generic_chunk(bool fp64, int kind, int rule, int mode, const LaunchArgs& a);
 
-// Per-instance small math, one CTA per instance.
+// Per-instance small math: one CTA per instance, or one warp per instance
+// (eight to a CTA) when every instance has n d^2 <= 256 (nm_max: the largest
+// n d^2 of the instances).
 cudaError_t launch_small(bool fp64, int kind, int which, const InstDev* insts, int count, int f64io, int write_out,
-                         cudaStream_t st);
+                         int64_t nm_max, cudaStream_t st);
 
 // Chunk scans spread over the GPU (mgb_scan.cu), for matrix instances with
 // d a multiple of 16.  `insts` are `count` instances of one dimension sorted

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
                         st.f0 = f0[j][q];
                         st.f1 = st.f2 = st.f3 = T(0);
 #pragma unroll
-                        for (int s = 0; s < BS; ++s) P[s][q] = fwd_step<T, RULE>(st, f[s][q], li + s, kc, cy);
+                        for (int s = 0; s < BS; ++s) P[s][q] = fwd_step<T, RULE, MODE != MODE_LOCAL>(st, f[s][q], li + s, kc, cy);
                         base[j][q] = st.base;
                         blo[j][q] = st.blo;
                         f0[j][q] = st.f0;

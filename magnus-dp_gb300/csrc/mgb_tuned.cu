@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
 #pragma unroll
                         for (int q = 0; q < EPT; ++q) {
                             const int el = tid + q * TNT, r = el / D, cc = el % D;
-                            const float P = fwd_step<float, RULE>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, fcy[q]);
+                            const float P = fwd_step<float, RULE, MODE != MODE_LOCAL>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, fcy[q]);
                             sP[l * D * P4 + r * P4 + cc] = P;
                             if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
                         }
