@@ -155,14 +155,20 @@ struct Alg<T, KIND_MATRIX> {
 template <class T>
 struct Alg<T, KIND_SC> {
     static constexpr unsigned kMul = 0x428Eu, kAdjL = 0x3950u, kAdjR = 0x5390u;
+    // x with its sign flipped when `neg` is 1 (an integer XOR: the sign
+    // differs between lanes, and a negation through the FP64 pipe would cost
+    // as much as the fused multiply-add it feeds)
+    __device__ __forceinline__ static double flip(double v, unsigned neg) {
+        return __longlong_as_double(__double_as_longlong(v) ^ ((long long)neg << 63));
+    }
+    __device__ __forceinline__ static float flip(float v, unsigned neg) {
+        return __int_as_float(__float_as_int(v) ^ (int)(neg << 31));
+    }
     template <class PX, class PY>
     __device__ __forceinline__ static T signed_sum(unsigned mask, const PX* x, const PY* y, int el) {
         T s = T(0);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const T t = (T)x[k] * (T)y[el ^ k];
-            s += ((mask >> (4 * el + k)) & 1u) ? -t : t;
-        }
+        for (int k = 0; k < 4; ++k) s = fma(flip((T)x[k], (mask >> (4 * el + k)) & 1u), (T)y[el ^ k], s);
         return s;
     }
     __device__ __forceinline__ static T one(int, int el) { return el == 0 ? T(1) : T(0); }
