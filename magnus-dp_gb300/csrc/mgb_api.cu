@@ -145,12 +145,15 @@ int rule_divisibility(int integrator) {
 // long chunks at every d; the plain form keeps shorter ones at large d,
 // where its slots are twice as large and its scans cost little.
 int default_K(const mgb_problem& p) {
-    // 4-element algebras (SpaceCurve, 2 x 2) with long sample runs: 1024.
-    // Their chunk kernel (one thread per chunk) is cheap per sample, while
-    // every chunk step of the FP64 scan costs n(n-1)/2 products on the
-    // 1/64-rate FP64 pipe; four times fewer steps, and still 64+ chunks per
-    // instance for the thread-per-chunk parallelism.
-    if ((p.kind == MGB_KIND_SPACECURVE || p.dim == 2) && p.samples - 1 >= 65536) return 1024;
+    // 4-element algebras (SpaceCurve, 2 x 2) in the mixed form with long
+    // sample runs: 1024.  Their FP32 chunk kernel (one thread per chunk) is
+    // cheap per sample, while every chunk step of the FP64 scan costs
+    // n(n-1)/2 products on the 1/64-rate FP64 pipe; four times fewer steps,
+    // and still 64+ chunks per instance for the thread-per-chunk parallelism.
+    // (The plain form's FP64 chunk kernel is the larger cost: it keeps 256
+    // and the parallelism.)
+    if ((p.kind == MGB_KIND_SPACECURVE || p.dim == 2) && p.precision == MGB_PRECISION_MIXED && p.samples - 1 >= 65536)
+        return 1024;
     if (p.kind == MGB_KIND_SPACECURVE || p.dim <= 32 || p.precision == MGB_PRECISION_MIXED) return 256;
     if (p.dim <= 64) return 128;
     return 64;

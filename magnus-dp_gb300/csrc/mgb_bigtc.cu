@@ -260,7 +260,10 @@ __device__ bool tc_pass(Pipe& pp, const float* __restrict__ X, const float* __re
 
 // ------------------------------------------------------------ prefix passes
 // PF: samples of loads in flight per thread (8; 4 in the three-CTA variant,
-// whose register budget is smaller)
+// whose register budget is smaller).  A sample's place in its rule block is
+// a compile-time constant: the forward sweep starts at position 1 and the
+// reverse one at Kp (a multiple of 4 for Boole, of 2 for Simpson; Trapezoid
+// and Riemann have no blocks), and both advance PF (a multiple of 4) at a time.
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
@@ -303,10 +306,10 @@ __device__ __forceinline__ void prefix_fwd(const float* __restrict__ F, float* _
                 const int li = l0 + u;
                 if (li <= Kp) {
                     float4 P;
-                    P.x = fwd_step<float, RULE, CY>(s[0], cur[u].x, li, kc, cy[0]);
-                    P.y = fwd_step<float, RULE, CY>(s[1], cur[u].y, li, kc, cy[1]);
-                    P.z = fwd_step<float, RULE, CY>(s[2], cur[u].z, li, kc, cy[2]);
-                    P.w = fwd_step<float, RULE, CY>(s[3], cur[u].w, li, kc, cy[3]);
+                    P.x = fwd_step<float, RULE, CY>(s[0], cur[u].x, 1 + u, kc, cy[0]);
+                    P.y = fwd_step<float, RULE, CY>(s[1], cur[u].y, 1 + u, kc, cy[1]);
+                    P.z = fwd_step<float, RULE, CY>(s[2], cur[u].z, 1 + u, kc, cy[2]);
+                    P.w = fwd_step<float, RULE, CY>(s[3], cur[u].w, 1 + u, kc, cy[3]);
                     if (keep) st4(Pj + (int64_t)li * m + e4, P);
                 }
             }
@@ -349,10 +352,10 @@ __device__ __forceinline__ void prefix_rev(const float* __restrict__ H, float* _
                 const int li = l0 - u;
                 if (li >= first) {
                     float4 g;
-                    g.x = rev_step<float, RULE>(s[0], cur[u].x, li, kc, cy[0]);
-                    g.y = rev_step<float, RULE>(s[1], cur[u].y, li, kc, cy[1]);
-                    g.z = rev_step<float, RULE>(s[2], cur[u].z, li, kc, cy[2]);
-                    g.w = rev_step<float, RULE>(s[3], cur[u].w, li, kc, cy[3]);
+                    g.x = rev_step<float, RULE>(s[0], cur[u].x, 4 * PF - u, kc, cy[0]);
+                    g.y = rev_step<float, RULE>(s[1], cur[u].y, 4 * PF - u, kc, cy[1]);
+                    g.z = rev_step<float, RULE>(s[2], cur[u].z, 4 * PF - u, kc, cy[2]);
+                    g.w = rev_step<float, RULE>(s[3], cur[u].w, 4 * PF - u, kc, cy[3]);
                     st4(G + (int64_t)li * m + e4, g);
                 }
             }

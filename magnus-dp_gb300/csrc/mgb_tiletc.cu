@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(TT, 2)
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         P[l][q] = 0.f;
-                        if (l < ge) P[l][q] = fwd_step<float, RULE, false>(fs[q], sF[(l * D + 4 * pig + q) * PF + pc], li0 + l, kc, zc);
+                        if (l < ge) P[l][q] = fwd_step<float, RULE, false>(fs[q], sF[(l * D + 4 * pig + q) * PF + pc], 1 + l, kc, zc);
                     }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {

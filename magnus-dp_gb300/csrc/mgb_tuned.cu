@@ -239,13 +239,19 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                     // samples outer, the thread's EPT elements inner: EPT
                     // independent dependency chains interleave
                     float* sj = st + (j - 1) * 3 * m;
-                    for (int l = 0; l < ge; ++l) {
+                    // groups start at positions = 1 mod 4 (G is a multiple
+                    // of 4), so a sample's place in its rule block is 1 + l
+                    // mod 4 (Riemann, the only rule starting at 0, has none)
 #pragma unroll
-                        for (int q = 0; q < EPT; ++q) {
-                            const int el = tid + q * TNT, r = el / D, cc = el % D;
-                            const float P = fwd_step<float, RULE, MODE != MODE_LOCAL>(fs[q], sF[l * D * P4 + r * P4 + cc], li0 + l, kc, fcy[q]);
-                            sP[l * D * P4 + r * P4 + cc] = P;
-                            if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
+                    for (int l = 0; l < G; ++l) {
+                        if (l < ge) {
+#pragma unroll
+                            for (int q = 0; q < EPT; ++q) {
+                                const int el = tid + q * TNT, r = el / D, cc = el % D;
+                                const float P = fwd_step<float, RULE, MODE != MODE_LOCAL>(fs[q], sF[l * D * P4 + r * P4 + cc], 1 + l, kc, fcy[q]);
+                                sP[l * D * P4 + r * P4 + cc] = P;
+                                if (MODE == MODE_VJP) tape[((int64_t)(j - 1) * L + li0 + l) * m + el] = P;
+                            }
                         }
                     }
 #pragma unroll
@@ -351,12 +357,15 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                     __syncthreads();
                     {
                         float* sj = st + (j - 1) * 3 * m;
-                        for (int l = ge - 1; l >= 0; --l) {
 #pragma unroll
-                            for (int q = 0; q < EPT; ++q) {
-                                const int el = tid + q * TNT, r = el / D, cc = el % D;
-                                const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
-                                sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, li0 + l, kc, rcy[q]);
+                        for (int l = G - 1; l >= 0; --l) {
+                            if (l < ge) {
+#pragma unroll
+                                for (int q = 0; q < EPT; ++q) {
+                                    const int el = tid + q * TNT, r = el / D, cc = el % D;
+                                    const float H = (j < n) ? sH[l * D * P1 + r * P1 + cc] : 0.f;
+                                    sG[l * D * P1 + r * P1 + cc] = rev_step<float, RULE>(rs[q], H, 1 + l, kc, rcy[q]);
+                                }
                             }
                         }
 #pragma unroll
