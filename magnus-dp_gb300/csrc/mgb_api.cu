@@ -506,6 +506,7 @@ void plan_fill(const Call& call, PlanCore& pc, const std::vector<Derived>& dv) {
         I.glx = g + v.Q;
         I.dt = (p.tf - p.t0) / (double)(p.samples - 1);
         I.dt_k = kernel_step(p, I.dt);
+        fill_rule_coefs(I);
         I.sig = (I.dt_k != 0.0) ? I.dt / I.dt_k : 1.0;
         I.S = (int64_t)p.samples;
         I.d = (p.kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p.dim;
@@ -1591,6 +1592,7 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
     I.glx = g + v.Q;
     I.dt = (p->tf - p->t0) / (double)(p->samples - 1);
     I.dt_k = kernel_step(*p, I.dt);
+    fill_rule_coefs(I);
     I.sig = (I.dt_k != 0.0) ? I.dt / I.dt_k : 1.0;
     I.S = (int64_t)p->samples;
     I.d = (p->kind == MGB_KIND_SPACECURVE) ? 2 : (int32_t)p->dim;

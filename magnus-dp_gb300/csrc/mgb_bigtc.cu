@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(TNT, MINB)
         const bool riem0 = (RULE == R_RIEMANN) && c == 0;
         const int first = riem0 ? 0 : 1;
         const int64_t Lm = (int64_t)L * m, nm = (int64_t)n * m;
-        const RuleCoef<float> kc(I.dt_k);
+        const RuleCoef<float> kc = rule_coef<float>(I);
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         float* const tape = slot;               // [n-1][L][m] P_j
         float* const Wb = tape + (n - 1) * Lm;  // [L][m] level values

@@ -75,7 +75,30 @@ struct InstDev {
     int64_t S;
     int32_t d, m, n, C, Q, K, op;
     int32_t pad_;
+    // The rule coefficients of dt_k (RuleCoef's order), computed once on the
+    // host by rule_coefs(): FP64 divisions in every thread of every chunk
+    // took a large share of the 1/64-rate FP64 pipe.
+    double rcd[9];
+    float rcf[9];
+    int32_t pad2_;
 };
+
+// h, t3, c38, c98, c4_3, b14, b64, b24, dt of a step (host and device).
+__host__ __device__ inline void rule_coefs(double dtd, double* c) {
+    c[0] = dtd / 2;
+    c[1] = dtd / 3;
+    c[2] = 3 * dtd / 8;
+    c[3] = 9 * dtd / 8;
+    c[4] = 4 * dtd / 3;
+    c[5] = 14 * dtd / 45;
+    c[6] = 64 * dtd / 45;
+    c[7] = 24 * dtd / 45;
+    c[8] = dtd;
+}
+inline void fill_rule_coefs(InstDev& I) {
+    rule_coefs(I.dt_k, I.rcd);
+    for (int i = 0; i < 9; ++i) I.rcf[i] = (float)I.rcd[i];
+}
 
 // Chunk c of an instance: samples [b, e], e = min(b + K, S - 1).
 struct ChunkRef {
@@ -200,11 +223,16 @@ struct Alg<T, KIND_SC> {
 template <class T>
 struct RuleCoef {
     T h, t3, c38, c98, c4_3, b14, b64, b24, dt;
-    __device__ __forceinline__ explicit RuleCoef(double dtd)
-        : h((T)(dtd / 2)), t3((T)(dtd / 3)), c38((T)(3 * dtd / 8)), c98((T)(9 * dtd / 8)),
-          c4_3((T)(4 * dtd / 3)), b14((T)(14 * dtd / 45)), b64((T)(64 * dtd / 45)), b24((T)(24 * dtd / 45)),
-          dt((T)dtd) {}
+    __device__ __forceinline__ explicit RuleCoef(const T* c)
+        : h(c[0]), t3(c[1]), c38(c[2]), c98(c[3]), c4_3(c[4]), b14(c[5]), b64(c[6]), b24(c[7]), dt(c[8]) {}
 };
+// The instance's coefficients in the compute type (precomputed on the host).
+template <class T>
+__device__ __forceinline__ RuleCoef<T> rule_coef(const InstDev& I);
+template <>
+__device__ __forceinline__ RuleCoef<float> rule_coef<float>(const InstDev& I) { return RuleCoef<float>(I.rcf); }
+template <>
+__device__ __forceinline__ RuleCoef<double> rule_coef<double>(const InstDev& I) { return RuleCoef<double>(I.rcd); }
 
 // A chunk carry (FP64 on the host side) as an unevaluated sum hi + lo in the
 // compute type: exact for double, ~2x float precision for float.  Running

@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
         const int first = riem0 ? 0 : 1;
         const int64_t Lm = (int64_t)L * m;
         const int64_t nm = (int64_t)n * m;
-        const RuleCoef<T> kc(I.dt_k);
+        const RuleCoef<T> kc = rule_coef<T>(I);
 
         T* Ab = slot;             // [L][m]   A over the chunk
         T* tape = Ab + Lm;        // [n-1][L][m]  P_j over the chunk

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
         const int Kp = (int)(e - b);
         const bool riem0 = (RULE == R_RIEMANN) && c == 0;
         const int first = riem0 ? 0 : 1;
-        const RuleCoef<T> kc(I.dt_k);
+        const RuleCoef<T> kc = rule_coef<T>(I);
         const double* pic = I.pi + (int64_t)c * n * 4;
         const int NL = (MODE == MODE_LOCAL) ? n : n - 1;
 

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(TT, 2)
         const bool riem0 = (RULE == R_RIEMANN) && c == 0;
         const int first = riem0 ? 0 : 1;
         const int64_t nm = (int64_t)n * m;
-        const RuleCoef<float> kc(I.dt_k);
+        const RuleCoef<float> kc = rule_coef<float>(I);
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         float* const st = slot;  // [n][3][m] prefix state
 

@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
         const bool riem0 = (RULE == R_RIEMANN) && c == 0;
         const int first = riem0 ? 0 : 1;
         const int64_t nm = (int64_t)n * m;
-        const RuleCoef<float> kc(I.dt_k);
+        const RuleCoef<float> kc = rule_coef<float>(I);
         const double* pic = I.pi + (int64_t)c * nm;
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         const int NLf = (MODE == MODE_LOCAL) ? n : n - 1;  // levels with a forward prefix
