@@ -108,18 +108,35 @@ __global__ void __launch_bounds__(TT, 2)
             }
         __syncthreads();
 
+        // A of a group, (row r of the stacked 128 x 32 operand, 8-wide k
+        // chunk) items, NIT per thread, held in registers: the next group's
+        // loads are issued once this group is staged and land while its
+        // levels run
+        constexpr int NIT = 128 * (D / 8) / TT;
+        float av[NIT][8];
+        auto load_group = [&](int l0g) {
+            const int geg = min(G, Kp - l0g + 1);
+#pragma unroll
+            for (int ii = 0; ii < NIT; ++ii) {
+                const int it = tid + ii * TT, r = it % 128, k8 = it / 128, s = r / D, i = r % D;
+                float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
+                if (s < geg) {
+                    const float4* p = reinterpret_cast<const float4*>(Ag + (int64_t)(l0g + s) * m + i * D + k8 * 8);
+                    x0 = __ldg(p);
+                    x1 = __ldg(p + 1);
+                }
+                av[ii][0] = x0.x; av[ii][1] = x0.y; av[ii][2] = x0.z; av[ii][3] = x0.w;
+                av[ii][4] = x1.x; av[ii][5] = x1.y; av[ii][6] = x1.z; av[ii][7] = x1.w;
+            }
+        };
+        if (first <= Kp) load_group(first);
         for (int li0 = first; li0 <= Kp && alive; li0 += G) {
             const int ge = min(G, Kp - li0 + 1);
             // ---- group operands: A of the ge samples -> X pieces and W_1 (FP32)
-            for (int it = tid; it < 128 * (D / 8); it += TT) {
-                const int r = it % 128, k8 = it / 128, s = r / D, i = r % D;
-                float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                if (s < ge) {
-                    const float4* p = reinterpret_cast<const float4*>(Ag + (int64_t)(li0 + s) * m + i * D + k8 * 8);
-                    const float4 x0 = __ldg(p), x1 = __ldg(p + 1);
-                    v[0] = x0.x; v[1] = x0.y; v[2] = x0.z; v[3] = x0.w;
-                    v[4] = x1.x; v[5] = x1.y; v[6] = x1.z; v[7] = x1.w;
-                }
+#pragma unroll
+            for (int ii = 0; ii < NIT; ++ii) {
+                const int it = tid + ii * TT, r = it % 128, k8 = it / 128, s = r / D, i = r % D;
+                const float* v = av[ii];
                 float* f = sF + (s * D + i) * PF + k8 * 8;
                 reinterpret_cast<float4*>(f)[0] = make_float4(v[0], v[1], v[2], v[3]);
                 reinterpret_cast<float4*>(f)[1] = make_float4(v[4], v[5], v[6], v[7]);
@@ -138,6 +155,7 @@ __global__ void __launch_bounds__(TT, 2)
                 for (int pcs = 0; pcs < 3; ++pcs)
                     *reinterpret_cast<uint4*>(xs + pcs * TILE + o) = make_uint4(wv[pcs][0], wv[pcs][1], wv[pcs][2], wv[pcs][3]);
             }
+            if (li0 + G <= Kp) load_group(li0 + G);
             __syncthreads();
 
             // prefix state of a level (this thread's elements; it alone
