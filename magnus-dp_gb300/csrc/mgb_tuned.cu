@@ -33,8 +33,8 @@ struct TileCfg {
     static constexpr int P4 = D + 4;              // 16-byte aligned pitch
     static constexpr int P1 = D + 1;              // odd pitch (column reads)
     static constexpr int EPT = m / TNT;           // prefix elements per thread
-    // forward: A^T, P, f; reverse: A (two buffers), P^T, G, H
-    static constexpr int OPND = 3 * G * D * P4 + 2 * G * D * P1;
+    static constexpr int OPND = (3 * G * D * P4 > 2 * G * D * P4 + 2 * G * D * P1) ? 3 * G * D * P4
+                                                                                   : 2 * G * D * P4 + 2 * G * D * P1;
     static_assert(G * TPS == TNT, "tile mapping");
     static_assert(EPT >= 1 && EPT * TNT == m, "prefix mapping");
 };
@@ -110,7 +110,6 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
     float* const sPT = sA + G * D * P4;  // reverse: P^T   [G][D][P4]
     float* const sG = sPT + G * D * P4;  // reverse: G     [G][D][P1]
     float* const sH = sG + G * D * P1;   // reverse: H     [G][D][P1]
-    float* const sA1 = sH + G * D * P1;  // reverse: the next group's A (asynchronous copy)
     float* const slot = scratch + (int64_t)blockIdx.x * slot_elems;
 
     const int tid = threadIdx.x;
@@ -317,35 +316,17 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                     rcy[q].lo = cyt[((int64_t)(n + j - 1) * 2 + 1) * m + el];
                 }
             };
-            // A of a group goes to shared memory by asynchronous copies
-            // issued one group ahead into the other of two buffers; the
-            // level-(n-1) tape of the next group is loaded during this
-            // group's last level.  Rows of a partial group beyond ge are
-            // never read (products run for tl < ge only).
-            auto copy_group_A = [&](float* dst, int l0g) {
-                const int nvalid = min(G, Kp - l0g + 1) * m;
+            for (int li0 = last0; li0 >= first; li0 -= G) {
+                const int ge = min(G, Kp - li0 + 1);
+                load_group(va, Ag + (int64_t)li0 * m, ge * m, true);
+                if (n > 1) load_group(vt, tape + ((int64_t)(n - 2) * L + li0) * m, ge * m, false);
+                load_rstate(n);
 #pragma unroll
                 for (int q = 0; q < NV; ++q) {
                     const int i4 = tid + q * TNT;
-                    if (i4 * 4 < nvalid) {
-                        const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                        const uint32_t sa = (uint32_t)__cvta_generic_to_shared(dst + l * D * P4 + r * P4 + cc);
-                        const float* src = Ag + (int64_t)l0g * m + (int64_t)i4 * 4;
-                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(src) : "memory");
-                    }
+                    const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                    *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = va[q];
                 }
-                asm volatile("cp.async.commit_group;" ::: "memory");
-            };
-            copy_group_A(sA, last0);
-            if (n > 1) load_group(vt, tape + ((int64_t)(n - 2) * L + last0) * m, min(G, Kp - last0 + 1) * m, false);
-            int buf = 0;
-            for (int li0 = last0; li0 >= first; li0 -= G) {
-                const int ge = min(G, Kp - li0 + 1);
-                float* const sAc = buf ? sA1 : sA;
-                asm volatile("cp.async.wait_group 0;" ::: "memory");
-                if (li0 - G >= first) copy_group_A(buf ? sA : sA1, li0 - G);
-                buf ^= 1;
-                load_rstate(n);
                 float dacc[4][4] = {};
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
@@ -363,10 +344,9 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                         __syncthreads();
                         load_rstate(j);
                         if (j > 1) load_group(vt, tape + ((int64_t)(j - 2) * L + li0) * m, ge * m, false);
-                        else if (li0 - G >= first) load_group(vt, tape + ((int64_t)(n - 2) * L + li0 - G) * m, G * m, false);
                         if (tl < ge) {
                             float hacc[4][4] = {};
-                            mma_adjL<D>(hacc, sAc + tl * D * P4, sG + tl * D * P1, r0, c0);
+                            mma_adjL<D>(hacc, sA + tl * D * P4, sG + tl * D * P1, r0, c0);
                             mma_adjR<D>(dacc, sG + tl * D * P1, sPT + tl * D * P4, r0, c0);
 #pragma unroll
                             for (int t = 0; t < 4; ++t)
