@@ -253,6 +253,7 @@ struct Call {
     const void* const* ckpt_in;  // vjp, nullable array
     void* const* dA;             // vjp
     cudaStream_t stream;
+    int budget_parts = 1;        // plans that will be resident at once (their scratch budgets share the memory)
 };
 
 // ---------------------------------------------------------------- plans
@@ -374,7 +375,10 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
     // segments: runs of equal dimension
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    size_t budget = std::max<size_t>((size_t)256 << 20, std::min<size_t>(free_b / 2, (size_t)48 << 30));
+    // up to half the free memory, at most 96 GB (a two-CTA d = 128 segment asks
+    // ~51 GB at n = 6), shared by the plans resident at once
+    size_t budget = std::max<size_t>((size_t)256 << 20,
+                                     std::min<size_t>(free_b / 2, (size_t)96 << 30) / (size_t)std::max(1, call.budget_parts));
     // MGB_SCRATCH_MB: a fixed scratch budget in MiB (tests use it to make the
     // segments' slot counts shrink below their asks)
     if (const char* ev = std::getenv("MGB_SCRATCH_MB"))
@@ -1319,6 +1323,7 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
         u.call.cot = u.cot.data();
         u.call.dA = u.dA.data();
         u.call.ckpt_out = u.ck.data();
+        u.call.budget_parts = NS;
         st = plan_layout(u.call, u.pc, u.dv);
         plan_slot = std::max(plan_slot, u.pc.bytes);
     }
