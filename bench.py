@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--workload", default="config4", choices=["config4", "config1", "config2", "config3"],
                     help="config4 = the headline fwd+VJP line; the others print their own measurement lines")
     ap.add_argument("--instances", type=int, default=0, help="config3: number of instances (0 = all 10000)")
+    ap.add_argument("--dim", type=int, default=64, help="config2: matrix dimension (64 is the configuration; "
+                                                         "128 profiles the d = 128 tensor-core kernel)")
     return ap.parse_args()
 
 
@@ -287,7 +289,7 @@ def run_config2(args):
     from magnus_gb300 import _lib, workloads
     lib = _lib.load()
     dev = torch.device("cuda", 0)
-    B, S, n, d = (args.batch if args.batch != CONFIG4["batch"] else 256), 16385, 4, 64
+    B, S, n, d = (args.batch if args.batch != CONFIG4["batch"] else 256), 16385, 4, args.dim
     Sk = workloads.config2_coeffs(seed=2, batch=B, d=d)
     A = workloads.config2_samples_torch(Sk, samples=S, device=dev)
     out = torch.empty((B, d, d), dtype=torch.float32, device=dev)
@@ -298,7 +300,7 @@ def run_config2(args):
     autotune = _describe(lib, plan)
     ms = _time_graph(torch, lambda: _lib.check(lib.mgb_plan_forward(plan, ct.c_void_p(torch.cuda.current_stream().cuda_stream))), args.steps)
     lib.mgb_plan_destroy(plan)
-    sub = 4
+    sub = min(4, B)
     st = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
     res = {}
     for prec in (_lib.PRECISION_MIXED, _lib.PRECISION_PLAIN):
@@ -316,7 +318,7 @@ def run_config2(args):
     flops = (n - 1) * 2.0 * d ** 3 * S * B
     tf = flops / (ms / 1e3) / 1e12
     fp32_peak = 152 * 128 * 2 * load_peaks()[2] * 1e6 / 1e12
-    print(json.dumps({"workload": "config2: 256 x d=64 skew A(t), S=16385, Boole, n=4, sum, float32, forward",
+    print(json.dumps({"workload": f"config2: {B} x d={d} skew A(t), S=16385, Boole, n=4, sum, float32, forward",
                       "metric": "samples·order/s forward", "value": B * S * n / (ms / 1e3), "ms": ms,
                       "precision": "mixed", "fp32_simt": {"achieved_tflops": tf, "nominal_peak_tflops": fp32_peak,
                                                           "frac": tf / fp32_peak},
