@@ -85,6 +85,27 @@ def test_checkpoint_bytes():
     assert lib.mgb_checkpoint_bytes(ctypes.byref(_prob(n=0))) == 0
 
 
+def test_default_checkpoint_interval():
+    """Default K (checkpoint_K = 0): 256, except 1024 for mixed-form 4-element
+    algebras (SpaceCurve, 2 x 2) with at least 65537 samples; read back
+    through the checkpoint size (2C + 1) * n * m doubles."""
+    lib = _lib.load()
+
+    def chunks(**kw):
+        p = _prob(**kw)
+        n, m = p.n, 4 if kw.get("kind") == _lib.KIND_SPACECURVE else p.dim * p.dim
+        return (lib.mgb_checkpoint_bytes(ctypes.byref(p)) // (8 * n * m) - 1) // 2
+
+    big = 65537
+    assert chunks(samples=big, precision=_lib.PRECISION_MIXED, dtype_code=_lib.DTYPE_F32) == 64
+    assert chunks(samples=big, precision=_lib.PRECISION_MIXED, dtype_code=_lib.DTYPE_F32,
+                  kind=_lib.KIND_SPACECURVE) == 64
+    assert chunks(samples=big, precision=_lib.PRECISION_PLAIN) == 256
+    assert chunks(samples=big - 4, precision=_lib.PRECISION_MIXED, dtype_code=_lib.DTYPE_F32) == 256
+    assert chunks(samples=big, precision=_lib.PRECISION_MIXED, dtype_code=_lib.DTYPE_F32, dim=4) == 256
+    assert chunks(samples=big, precision=_lib.PRECISION_MIXED, dtype_code=_lib.DTYPE_F32, checkpoint_K=128) == 512
+
+
 def test_gl_table_replace_and_max_order():
     import magnus_gb300 as mg
     assert mg.max_order() == 64
