@@ -328,22 +328,12 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                     *reinterpret_cast<float4*>(sA + l * D * P4 + r * P4 + cc) = va[q];
                 }
                 float dacc[4][4] = {};
+                // two barriers per level: P^T of the next level is staged in
+                // this level's prefix phase (its products have finished
+                // reading sPT at the first barrier)
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
-                        // P_j (row-major on the tape) -> P^T in shared memory
-#pragma unroll
-                        for (int q = 0; q < NV; ++q) {
-                            const int i4 = tid + q * TNT;
-                            const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
-                            float* pt = sPT + l * D * P4 + r;
-                            pt[(cc + 0) * P4] = vt[q].x;
-                            pt[(cc + 1) * P4] = vt[q].y;
-                            pt[(cc + 2) * P4] = vt[q].z;
-                            pt[(cc + 3) * P4] = vt[q].w;
-                        }
-                        __syncthreads();
                         load_rstate(j);
-                        if (j > 1) load_group(vt, tape + ((int64_t)(j - 2) * L + li0) * m, ge * m, false);
                         if (tl < ge) {
                             float hacc[4][4] = {};
                             mma_adjL<D>(hacc, sA + tl * D * P4, sG + tl * D * P1, r0, c0);
@@ -375,6 +365,22 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
                             sj[m + el] = rs[q].rlo;
                             sj[2 * m + el] = rs[q].pend;
                         }
+                    }
+                    if (j > 1) {
+                        // P_{j-1} (row-major on the tape) -> P^T in shared
+                        // memory for the next level; then the tape of the
+                        // level after it
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) {
+                            const int i4 = tid + q * TNT;
+                            const int l = (i4 * 4) / m, el = (i4 * 4) % m, r = el / D, cc = el % D;
+                            float* pt = sPT + l * D * P4 + r;
+                            pt[(cc + 0) * P4] = vt[q].x;
+                            pt[(cc + 1) * P4] = vt[q].y;
+                            pt[(cc + 2) * P4] = vt[q].z;
+                            pt[(cc + 3) * P4] = vt[q].w;
+                        }
+                        if (j > 2) load_group(vt, tape + ((int64_t)(j - 3) * L + li0) * m, ge * m, false);
                     }
                     __syncthreads();
                 }
