@@ -11,10 +11,12 @@
 //     sequential over the chunk's samples) alternates with a product pass
 //     (flat over sample x element).  Chunk buffers live in a per-CTA slot of
 //     global scratch memory.
-//   k_scan         one CTA per instance: pi^{c+1} = Chen(Lambda^c, pi^c), FP64.
-//   k_fin_fwd      one CTA per instance: D^(q), E, Omega and the output.
-//   k_fin_vjp      one CTA per instance: cotangents tau_j on the totals T_j.
-//   k_rscan        one CTA per instance: rho for every chunk (reverse scan).
+//   k_scan         pi^{c+1} = Chen(Lambda^c, pi^c), FP64.
+//   k_fin_fwd      D^(q), E, Omega and the output.
+//   k_fin_vjp      cotangents tau_j on the totals T_j.
+//   k_rscan        rho for every chunk (reverse scan).
+//     One CTA per instance, or one warp per instance when n d^2 <= 256
+//     (k_scan_w / k_rscan_w for the scans: step state in shared memory).
 #include "mgb_common.cuh"
 #include "mgb_kernels.h"
 
