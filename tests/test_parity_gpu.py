@@ -258,3 +258,32 @@ def test_big_mixed_kernel_float32(integrator, S, d, cuda):
     g = core.compute_vjp(n, A, cot, t0=0.0, tf=1.0, op="sum", integrator=integrator, precision="mixed",
                          checkpoint_K=32)
     assert rel(g, gref) <= 1e-6, rel(g, gref)
+
+
+def test_mixed_long_four_element_problems_use_long_chunks(cuda):
+    """Mixed-form 2x2 and SpaceCurve problems with >= 65537 samples run with
+    1024-sample chunks by default (fewer FP64 scan steps); forward and VJP
+    stay within 1e-6 of the FP64 oracle."""
+    from magnus_gb300 import workloads
+    S = 65537
+    A = workloads.config0_samples(seed=5, d=2, samples=S)
+    ref = O.forward(A, 5, 0.0, 1.0, "many", "Boole")
+    out = core.compute(5, A, 0.0, 1.0, op="many", integrator="Boole", precision="mixed")
+    for k in range(5):
+        assert rel(out[k], ref[k]) <= 1e-6, (k, rel(out[k], ref[k]))
+    cot = np.random.default_rng(5).standard_normal((2, 2))
+    gref = O.vjp(A, cot, 5, 0.0, 1.0, "sum", "Boole")
+    g = core.compute_vjp(5, A, cot, t0=0.0, tf=1.0, op="sum", integrator="Boole", precision="mixed")
+    assert rel(g, gref) <= 1e-6, rel(g, gref)
+
+    F = workloads.config1_samples_np(*workloads.config1_coeffs(seed=12, batch=1), samples=S, dtype=np.float64)[0]
+    ref = O.forward_sc(F, 6, 0.0, 2.0, "many", "Simpson")
+    out = core.compute_sc(6, F, 0.0, 2.0, op="many", integrator="Simpson", precision="mixed")
+    scale = max(np.linalg.norm(r) for r in ref)
+    for k in range(6):
+        den = np.linalg.norm(ref[k]) if np.linalg.norm(ref[k]) >= 1e-6 * scale else scale
+        assert np.linalg.norm(out[k] - ref[k]) / den <= 1e-6, k
+    cot = np.random.default_rng(6).standard_normal((6, 3))
+    gref = O.vjp_sc(F, cot, 6, 0.0, 2.0, "many", "Simpson")
+    g = core.compute_sc_vjp(6, F, cot, t0=0.0, tf=2.0, op="many", integrator="Simpson", precision="mixed")
+    assert rel(g, gref) <= 1e-6, rel(g, gref)
