@@ -139,6 +139,10 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= nslots) return;
     T* const tape = scratch + tid * slot_elems;  // [L][NMAX-1][4] prefix values P_j
+    // VJP: the chunk carries pi^c and rho^c split into hi + lo once per chunk,
+    // [4][NMAX][4] at the slot's end (a split in every rule block ran FP64
+    // conversions on the 1/64-rate pipe for every sample)
+    T* const cya = scratch + tid * slot_elems + slot_elems - 16 * NMAX;
 
     for (int64_t w = tid; w < nwork; w += nslots) {
         const ChunkRef wk = work[w];
@@ -152,6 +156,17 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
         const RuleCoef<T> kc = rule_coef<T>(I);
         const double* pic = I.pi + (int64_t)c * n * 4;
         const int NL = (MODE == MODE_LOCAL) ? n : n - 1;
+        if (MODE == MODE_VJP) {
+            const double* rcc = I.rho + (int64_t)c * n * 4;
+            for (int jq = 0; jq < n * 4; ++jq) {
+                const Carry<T> f = split_carry<T>(riem0 ? 0.0 : pic[jq]);
+                const Carry<T> r = split_carry<T>(rcc[jq]);
+                cya[jq] = f.hi;
+                cya[4 * NMAX + jq] = f.lo;
+                cya[8 * NMAX + jq] = r.hi;
+                cya[12 * NMAX + jq] = r.lo;
+            }
+        }
 
         // ---------------- forward over the chunk ----------------
         T base[NMAX][4], blo[NMAX][4], f0[NMAX][4];
@@ -187,7 +202,11 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
                     T P[BS][4];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
-                        const Carry<T> cy = split_carry<T>((MODE == MODE_LOCAL || riem0) ? 0.0 : pic[j * 4 + q]);
+                        Carry<T> cy{T(0), T(0)};
+                        if (MODE == MODE_VJP) {
+                            cy.hi = cya[j * 4 + q];
+                            cy.lo = cya[4 * NMAX + j * 4 + q];
+                        }
                         FwdState<T> st;
                         st.base = base[j][q];
                         st.blo = blo[j][q];
@@ -222,7 +241,6 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
         }
 
         if (MODE == MODE_VJP) {
-            const double* rc = I.rho + (int64_t)c * n * 4;
             T Rb[NMAX][4], rlo[NMAX][4], pend[NMAX][4];
 #pragma unroll
             for (int j = 0; j < NMAX; ++j)
@@ -260,7 +278,7 @@ __global__ void __launch_bounds__(SNT) k_small(const InstDev* __restrict__ insts
                         }
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
-                            const Carry<T> cy = split_carry<T>(rc[j * 4 + q]);
+                            const Carry<T> cy{cya[8 * NMAX + j * 4 + q], cya[12 * NMAX + j * 4 + q]};
                             RevState<T> st;
                             st.Rb = Rb[j][q];
                             st.rlo = rlo[j][q];

@@ -573,7 +573,8 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
     TunedChoice tc = choose_tuned(plain, kind, rule, MODE_VJP, f64io, hi, 0);
     int64_t want;
     if (tc.use && tc.family == 1) {
-        sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4;  // one thread's tape
+        // one thread's tape, then its chunk carries split to hi + lo (VJP)
+        sz.slot_elems = Lmax * (small_family_max_levels() - 1) * 4 + 16 * small_family_max_levels();
         want = std::min<int64_t>(nwork, (int64_t)sms * 1024);
     } else if (tc.use) {
         int cps = tc.ctas_per_sm;
