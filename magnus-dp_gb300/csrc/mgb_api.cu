@@ -204,7 +204,7 @@ mgb_status validate(const mgb_problem* p, size_t gl_max, Derived* dv) {
     return MGB_OK;
 }
 
-size_t ckpt_doubles(const mgb_problem& p, const Derived& dv) { return (size_t)(2 * dv.C + 1) * dv.nm; }
+size_t ckpt_doubles(const mgb_problem&, const Derived& dv) { return (size_t)(2 * dv.C + 1) * dv.nm; }
 size_t ws_doubles(const Derived& dv) { return (size_t)dv.C * dv.nm + 3 * (size_t)dv.Q * dv.nm + 6 * (size_t)dv.nm; }
 
 // Step used inside the chunk kernels (see InstDev::dt_k): the plain form
