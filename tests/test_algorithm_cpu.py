@@ -9,7 +9,10 @@ checked against the oracle (the reference's per-node recursion) on the CPU:
   sum_{m<j} Lambda^c_{j-m} pi^c_m (Chen's identity);
 * the adjoint: tau_j from the small algebra, then P-bar_j = tau_j at the last
   sample + A^T W-bar_{j+1}, W-bar_j = prefix^T(P-bar_j),
-  dA = W-bar_1 + sum_j W-bar_{j+1} P_j^T.
+  dA = W-bar_1 + sum_j W-bar_{j+1} P_j^T;
+* the mixed form's step dt_k (rule weights exact in FP32) and the rescaling
+  of level j by (dt/dt_k)^j;
+* SpaceCurves as the associative quaternion recursion with signed levels.
 
 The block rules are stated as explicit (S x S) prefix matrices, so prefix^T is
 their transpose.  Reference rules: src/integration/boole.hpp:24-74,
@@ -195,3 +198,63 @@ def test_adjoint_equals_reference_vjp(rule, op):
     dA += Wbar_next
     ref = O.vjp(A, cot, n, 0.0, 1.0, op, rule)
     assert np.linalg.norm(dA - ref) / np.linalg.norm(ref) <= 1e-12
+
+
+@pytest.mark.parametrize("rule,u", [("Boole", 90.0), ("Simpson", 6.0), ("Trapezoid", 2.0), ("Riemann", 1.0)])
+def test_mixed_step_rescaling(rule, u):
+    """The mixed form integrates with dt_k = u 2^round(log2(dt/u)) (every rule
+    weight dt_k c/u exact in FP32) and rescales the totals by
+    (dt/dt_k)^j: level j is homogeneous of degree j in the step."""
+    rng = np.random.default_rng(4)
+    S = 33 if rule != "Riemann" else 30
+    A = rng.standard_normal((S, 2, 2))
+    dt = 0.7 / (S - 1)
+    dtk = u * 2.0 ** np.round(np.log2(dt / u))
+    for c in {"Boole": [1 / 2, 1 / 3, 3 / 8, 9 / 8, 4 / 3, 14 / 45, 64 / 45, 24 / 45], "Simpson": [1 / 2, 1 / 3, 4 / 3],
+              "Trapezoid": [1 / 2], "Riemann": [1.0]}[rule]:
+        w = dtk * c
+        assert np.float32(w) == w  # exact in FP32
+    T = [Pj[-1] for Pj in levels(A, 4, prefix_matrix(S, dt, rule))]
+    Tk = [Pj[-1] for Pj in levels(A, 4, prefix_matrix(S, dtk, rule))]
+    sig = dt / dtk
+    for j in range(4):
+        assert np.allclose(Tk[j] * sig ** (j + 1), T[j], rtol=1e-13, atol=1e-15 * np.abs(T[j]).max())
+
+
+def test_spacecurve_product_is_negated_quaternion_product():
+    """The reference's SpaceCurve product c = (a.b, -b0 a + a x b) on padded
+    (0, a) equals -qmul(a, b), qmul(a, b) = b (x) a (Hamilton), so the
+    recursion runs on the associative qmul with level signs (-1)^(k-1)."""
+    rng = np.random.default_rng(5)
+
+    def hamilton(p, q):
+        p0, pv, q0, qv = p[0], p[1:], q[0], q[1:]
+        return np.concatenate([[p0 * q0 - pv @ qv], p0 * qv + q0 * pv + np.cross(pv, qv)])
+
+    for _ in range(20):
+        a = np.concatenate([[0.0], rng.standard_normal(3)])
+        b = rng.standard_normal(4)
+        ref_c = np.concatenate([[a[1:] @ b[1:]], -b[0] * a[1:] + np.cross(a[1:], b[1:])])
+        assert np.allclose(ref_c, -hamilton(b, a), atol=1e-14)
+    # the whole recursion: SpaceCurve data through the oracle equals the
+    # associative recursion on qmul with signed outputs
+    F = rng.standard_normal((33, 3)) * 0.5
+    n = 4
+    ref = O.forward_sc(F, n, 0.0, 1.0, "many", "Boole")
+    S = F.shape[0]
+    R = prefix_matrix(S, 1.0 / (S - 1), "Boole")
+    A4 = np.concatenate([np.zeros((S, 1)), F], axis=1)
+    P, W = [], A4
+    for _ in range(n):
+        Pj = R @ W
+        P.append(Pj)
+        W = np.array([hamilton(p, a) for a, p in zip(A4, Pj)])  # qmul(a, p) = p (x) a
+    # qmul-algebra small forward: represent quaternions by their 4x4 right-multiplication matrices
+    def rmat(q):
+        return np.array([hamilton(np.eye(4)[k], q) for k in range(4)]).T  # x -> x (x) q
+    T = [rmat(Pj[-1]) for Pj in P]
+    Om, _, _ = small_forward(T, n)
+    for k in range(n):
+        q = Om[k] @ np.eye(4)[0]  # the quaternion itself: 1 (x) q
+        sign = (-1) ** k
+        assert np.allclose(sign * q[1:], ref[k], rtol=1e-12, atol=1e-13 * np.abs(ref).max())
