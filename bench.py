@@ -25,6 +25,7 @@ import argparse
 import ctypes
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -157,6 +158,25 @@ def cpu_sample(instances, samples, threads, repeats=1):
     return instances * samples * c["n"] / best, best
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu / /proc/cpuinfo), for the CPU legs."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -178,7 +198,8 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "config4 fwd+VJP (bounded CPU sample)", "batch": CONFIG4["batch"],
                        "samples": CONFIG4["samples"], "dim": CONFIG4["d"], "n": CONFIG4["n"]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -670,7 +691,7 @@ def main():
         cpu_value, cpu_s = cpu_sample(inst, args.cpu_samples, threads)
         result["cpu_baseline"] = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": f"{inst} config4 trajectories at S={args.cpu_samples} (of 32769), "
-                                            f"fwd + VJP, float32, {cpu_s:.1f} s"}
+                                            f"fwd + VJP, float32, {cpu_s:.1f} s", "cpu_model": cpu_model()}
     if plan is not None and plan.value:
         _lib.check(lib.mgb_plan_destroy(plan))
     if rank == 0:
