@@ -168,7 +168,9 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
  * array and it keeps the previous call's contents (nothing needs clearing);
  * calls whose GPU work can overlap race on it, so order them on one stream.
  * No counterpart in the reference (its CPU code allocates on the host heap).
- * A and out are device pointers; the call is stream-ordered. */
+ * A and out are device pointers; the call is stream-ordered and enqueues
+ * kernels only: the problem's descriptor and Gauss-Legendre values travel as
+ * kernel parameters, so no host-to-device copy makes it wait for the stream. */
 #define MGB_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, void* out, void* stream);
 

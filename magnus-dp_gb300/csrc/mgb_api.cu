@@ -1507,8 +1507,24 @@ static_assert(kNoAllocBytes == MGB_NOALLOC_SCRATCH_BYTES, "keep the header const
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-__global__ void k_noalloc_work(ChunkRef* work, int C) {
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) work[c] = ChunkRef{0, c};
+// The call's descriptor and Gauss-Legendre values travel as kernel
+// parameters, so the entry point enqueues kernels only: a host-to-device copy
+// from pageable host memory would make the driver wait for the stream.
+constexpr int kNoAllocGLSlice = 32;
+struct NoAllocGL {
+    double w[kNoAllocGLSlice];
+    double x[kNoAllocGLSlice];
+};
+
+__global__ void k_noalloc_setup(InstDev I, InstDev* dst, NoAllocGL gl, int q0, int nq, double* glw, double* glx,
+                                ChunkRef* work, int C) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0 && dst) *dst = I;
+    if (tid < nq) {
+        glw[q0 + tid] = gl.w[tid];
+        glx[q0 + tid] = gl.x[tid];
+    }
+    for (int c = tid; c < C; c += gridDim.x * blockDim.x) work[c] = ChunkRef{0, c};
 }
 
 std::mutex g_noalloc_mutex;
@@ -1568,8 +1584,6 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
                         " bytes of workspace; mgb_forward_noalloc is limited to MGB_NOALLOC_SCRATCH_BYTES (" +
                         std::to_string(kNoAllocBytes) + ")");
     const DevInfo di = device_info();
-    int64_t grid = std::min<int64_t>((int64_t)v.C, (int64_t)di.sms * 8);
-    grid = std::max<int64_t>(1, std::min<int64_t>(grid, (int64_t)((kNoAllocBytes - off_scr) / slot_bytes)));
 
     void* basev = nullptr;
     st = noalloc_base(&basev);
@@ -1608,25 +1622,43 @@ extern "C" mgb_status mgb_forward_noalloc(const mgb_problem* p, const void* A, v
     I.K = v.K;
     I.op = p->op;
     const size_t go = (size_t)v.Q * (v.Q - 1) / 2;
-    // pageable sources: each copy is staged before cudaMemcpyAsync returns
-    MGB_CUDA_TRY(cudaMemcpyAsync(base + off_inst, &I, sizeof(InstDev), cudaMemcpyHostToDevice, cs));
-    MGB_CUDA_TRY(cudaMemcpyAsync(g, gl->w.data() + go, (size_t)v.Q * sizeof(double), cudaMemcpyHostToDevice, cs));
-    MGB_CUDA_TRY(cudaMemcpyAsync(g + v.Q, gl->x.data() + go, (size_t)v.Q * sizeof(double), cudaMemcpyHostToDevice, cs));
+    InstDev* d_inst = reinterpret_cast<InstDev*>(base + off_inst);
     ChunkRef* d_work = reinterpret_cast<ChunkRef*>(base + off_work);
-    k_noalloc_work<<<(unsigned)std::min<int64_t>((v.C + 255) / 256, 1024), 256, 0, cs>>>(d_work, v.C);
-    MGB_CUDA_TRY(cudaGetLastError());
+    for (int q0 = 0; q0 < v.Q || q0 == 0; q0 += kNoAllocGLSlice) {
+        NoAllocGL sl;
+        std::memset(&sl, 0, sizeof(sl));
+        const int nq = std::min(kNoAllocGLSlice, v.Q - q0);
+        for (int q = 0; q < nq; ++q) {
+            sl.w[q] = gl->w[go + q0 + q];
+            sl.x[q] = gl->x[go + q0 + q];
+        }
+        const int C = q0 == 0 ? v.C : 0;
+        const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(((int64_t)C + 255) / 256, 1024));
+        k_noalloc_setup<<<blocks, 256, 0, cs>>>(I, q0 == 0 ? d_inst : nullptr, sl, q0, nq, g, g + v.Q, d_work, C);
+        MGB_CUDA_TRY(cudaGetLastError());
+    }
 
-    const InstDev* d_inst = reinterpret_cast<const InstDev*>(base + off_inst);
+    // Grid: as many CTAs (threads, for the one-thread-per-chunk kernel of
+    // 2 x 2 and SpaceCurve data) as a regular call would run, cut to the
+    // slots that fit in the array.  The thread-per-chunk kernel touches its
+    // slot only in the VJP, so its forward slots are the minimum it lays out.
+    const std::vector<InstDev> hi(1, I);
+    const TunedChoice tc = choose_tuned(plain, p->kind, p->integrator, MODE_LOCAL, f64io != 0, hi, 0);
+    int64_t slot_use = slot_elems;
+    if (tc.use && tc.family == 1) slot_use = 16 * (int64_t)small_family_max_levels();
+    const SegSizing sz = size_segment(plain, p->kind, p->integrator, f64io != 0, hi, v.C, di.sms, ~(size_t)0 >> 1);
+    const int64_t grid = std::max<int64_t>(
+        1, std::min<int64_t>(sz.grid, (int64_t)((kNoAllocBytes - off_scr) / ((size_t)slot_use * tsz))));
+
     LaunchArgs la;
     la.insts = d_inst;
     la.work = d_work;
     la.nwork = v.C;
     la.scratch = base + off_scr;
-    la.slot_elems = slot_elems;
+    la.slot_elems = slot_use;
     la.grid = grid;
     la.f64io = f64io;
     la.stream = cs;
-    const std::vector<InstDev> hi(1, I);
     MGB_CUDA_TRY(launch_chunk_any(plain, p->kind, p->integrator, MODE_LOCAL, la, hi, di.sms, 0));
     MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_SCAN, d_inst, 1, f64io, 0, (int64_t)p->n * v.m, cs));
     MGB_CUDA_TRY(launch_small(true, p->kind, SMALL_FIN_FWD, d_inst, 1, f64io, 1, (int64_t)p->n * v.m, cs));

@@ -44,8 +44,13 @@ def _problems(A, n, t0, tf, op, integrator, precision, kind, checkpoint_K):
     opc = _lib.OP_CODES.get(op)
     if opc is None:
         raise ValueError("could not deduce kernel op from str in Magnus::Dispatch::op_from_str(std::string_view)")
-    integ = _lib.INTEGRATOR_CODES["Boole" if integrator == "Auto" else integrator]
-    prob = _lib.make_problem(kind=kind, dtype_code=_DTYPES[A.dtype], precision=_lib.PRECISION_CODES[precision],
+    integ = _lib.INTEGRATOR_CODES.get("Boole" if integrator == "Auto" else integrator)
+    if integ is None:
+        raise ValueError("Could not resolve dispatch name option")
+    prec = _lib.PRECISION_CODES.get(precision)
+    if prec is None:
+        raise ValueError("Could not resolve dispatch name option")
+    prob = _lib.make_problem(kind=kind, dtype_code=_DTYPES[A.dtype], precision=prec,
                              op=opc, integrator=integ, n=n, samples=Ab.shape[1], dim=dim, t0=t0, tf=tf,
                              checkpoint_K=checkpoint_K)
     return batched, Ab, prob, dim

@@ -32,6 +32,17 @@ CASES = [
     ("mixed-f32-d32-sum", _lib.KIND_MATRIX, "float32", _lib.PRECISION_MIXED, _lib.OP_SUM, 0, 5, 2049, 32, 1e-6),
     ("plain-f64-spacecurve", _lib.KIND_SPACECURVE, "float64", _lib.PRECISION_PLAIN, _lib.OP_MANY, 1, 6, 1025, 2,
      1e-12),
+    # one thread per chunk (2 x 2 and SpaceCurve data) in FP32
+    ("mixed-f32-d2-many", _lib.KIND_MATRIX, "float32", _lib.PRECISION_MIXED, _lib.OP_MANY, 0, 5, 4097, 2, 1e-6),
+    ("mixed-f32-spacecurve", _lib.KIND_SPACECURVE, "float32", _lib.PRECISION_MIXED, _lib.OP_MANY, 1, 6, 4097, 2,
+     1e-6),
+    # the tensor-core kernel at d = 64: one 256-sample chunk slot takes half
+    # of the array, so the grid is cut to the single slot that fits
+    ("mixed-f32-d64-sum-one-slot", _lib.KIND_MATRIX, "float32", _lib.PRECISION_MIXED, _lib.OP_SUM, 0, 4, 1025, 64,
+     1e-6),
+    # n = 7: five Gauss-Legendre nodes
+    ("plain-f64-d4-n7-trapezoid", _lib.KIND_MATRIX, "float64", _lib.PRECISION_PLAIN, _lib.OP_ONE, 2, 7, 1025, 4,
+     1e-12),
 ]
 
 
