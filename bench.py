@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--e2e-batch", type=int, default=128)
     ap.add_argument("--cpu-instances", type=int, default=0, help="0 = one per host thread")
     ap.add_argument("--cpu-samples", type=int, default=4097)
+    ap.add_argument("--oracle-instances", type=int, default=4,
+                    help="instances of the timed batch whose mixed output and dA are checked against the "
+                         "FP64 oracle (full size, in the CPU leg)")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/cpu legs (quick runs)")
     ap.add_argument("--workload", default="config4", choices=["config4", "config1", "config2", "config3"],
                     help="config4 = the headline fwd+VJP line; the others print their own measurement lines")
@@ -158,6 +161,40 @@ def cpu_sample(instances, samples, threads, repeats=1):
     return instances * samples * c["n"] / best, best
 
 
+def _oracle_instance(job):
+    """FP64 forward (op sum) and VJP of one config4 instance by the collapsed
+    restatement of the reference recursion (oracle/collapsed.py)."""
+    import collapsed as Cl
+    A, cot, n, t0, tf = job
+    A64 = A.astype(np.float64)
+    return Cl.forward(A64, n, t0, tf, "sum", "Boole"), Cl.vjp(A64, cot.astype(np.float64), n, t0, tf, "sum", "Boole")
+
+
+def oracle_check(A, cot, out, dA, n, t0, tf):
+    """Relative Frobenius error of the engine's mixed output and dA (from the
+    timed steps) against the FP64 oracle on the same full-size instances;
+    one spawned worker per instance."""
+    import multiprocessing as mp
+    t = time.perf_counter()
+    jobs = [(A[i], cot[i], n, t0, tf) for i in range(A.shape[0])]
+    saved = os.environ.get("OPENBLAS_NUM_THREADS")
+    os.environ["OPENBLAS_NUM_THREADS"] = str(max(1, (os.cpu_count() or 1) // max(1, len(jobs))))
+    try:
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            refs = pool.map(_oracle_instance, jobs)
+    finally:
+        if saved is None:
+            os.environ.pop("OPENBLAS_NUM_THREADS", None)
+        else:
+            os.environ["OPENBLAS_NUM_THREADS"] = saved
+    ro = np.stack([r[0] for r in refs])
+    rg = np.stack([r[1] for r in refs])
+    e_out = float(np.linalg.norm(out.astype(np.float64) - ro) / np.linalg.norm(ro))
+    e_dA = float(np.linalg.norm(dA.astype(np.float64) - rg) / np.linalg.norm(rg))
+    return {"out": e_out, "dA": e_dA, "instances": len(jobs), "checker": "oracle/collapsed.py (FP64)",
+            "seconds": time.perf_counter() - t}
+
+
 def cpu_model():
     """The host CPU's model name (lscpu / /proc/cpuinfo), for the CPU legs."""
     try:
@@ -245,6 +282,72 @@ def _time_graph(torch, fn, steps, warmup=3):
     torch.cuda.synchronize()
     del g
     return e0.elapsed_time(e1) / steps
+
+
+def kernel_roofs(kernels, steps, B, S, d, n, K, plain=False):
+    """Roofline of each timed kernel of the config4 step (CUDA-event times
+    from the library's launch timing), per launch:
+
+      chunk_local  (n-1) products of 2 d^3 flop per sample; reads A once
+      chunk_vjp    3 (n-1) products per sample (replay, A^T G, G P^T); reads
+                   A twice, writes dA
+      scan, rscan  n(n-1)/2 d x d products per chunk step; read the chunk
+                   transfers, write the chunk states (FP64 arrays)
+      fin_*        the per-instance FP64 algebra (latency-bound, no roof)
+
+    Mixed-form products on the tensor cores are FP32-accurate emulations from
+    BF16 pieces, so their roof is the measured sustained BF16 rate / 3 (the
+    three-product BF16x3 convention).  The mixed-form scans run double-FP32
+    arithmetic on the FP32 pipes (about six FP32 flops per emulated flop):
+    roof = nominal FP32 rate (152 SMs x 128 lanes x 2 x max clock) / 6.  The
+    plain form's products and scans are rated against the nominal FP64 rate
+    (1.25 TFLOP/s; no measured peak).  bound = the roof the kernel is closer
+    to; frac = achieved / that roof's peak."""
+    hbm_peak, _, sm_max, src = load_peaks()
+    fp32_nominal = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp64_nominal = 1.25
+    m = d * d
+    C = -(-(S - 1) // K)
+    if plain:
+        prod_roof = (fp64_nominal, "fp64", "nominal FP64")
+        scan_roof = prod_roof
+    else:
+        prod_roof = (bf16_sustained_peak() / 3, "tensor", "BF16x3 = measured sustained BF16 / 3")
+        scan_roof = (fp32_nominal / 6, "fp32", "double-FP32 = nominal FP32 / 6")
+    work = {
+        "chunk_local": ((n - 1) * 2.0 * d ** 3 * S * B, S * m * 4.0 * B, prod_roof),
+        "chunk_vjp": (3 * (n - 1) * 2.0 * d ** 3 * S * B, 3 * S * m * 4.0 * B, prod_roof),
+        "scan": (n * (n - 1) / 2 * 2.0 * d ** 3 * C * B, (2 * C + 1) * n * m * 8.0 * B, scan_roof),
+        "rscan": (n * (n - 1) / 2 * 2.0 * d ** 3 * C * B, (2 * C) * n * m * 8.0 * B, scan_roof),
+    }
+    out = {}
+    for name, (launches, total_ms) in kernels.items():
+        launch_ms = total_ms / max(launches, 1)
+        per = launches / steps  # launches per step
+        flops, nbytes, (fpeak, fbound, fsrc) = work.get(name, (0.0, 0.0, (None, None, None)))
+        flops, nbytes = flops / per, nbytes / per
+        t = launch_ms / 1e3
+        tf = flops / t / 1e12 if flops else 0.0
+        gbs = nbytes / t / 1e9 if nbytes else 0.0
+        cfrac = tf / fpeak if fpeak else 0.0
+        hfrac = gbs / hbm_peak
+        if fpeak and cfrac >= hfrac:
+            r = {"bound": fbound, "achieved": tf, "peak": fpeak, "unit": "TFLOP/s", "frac": cfrac, "peak_source": fsrc}
+        else:
+            r = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hfrac,
+                 "peak_source": src + " HBM copy"}
+        r.update({"ms_per_step": total_ms / steps, "launch_ms": launch_ms, "launches_per_step": per,
+                  "compute_frac": cfrac, "hbm_frac": hfrac, "flops_per_launch": flops, "bytes_per_launch": nbytes})
+        out[name] = r
+    return out
+
+
+def bf16_sustained_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("bf16_tflops_sustained", 1700.0)
+    return 1700.0
 
 
 def _order_errors(mixed, plain):
@@ -445,6 +548,69 @@ def run_config3(args):
                       "autotune_picks": picks}))
 
 
+def config3_subset(torch, lib, _lib, dev, per_d=2):
+    """Config3's mixed-over-plain target on a fixed subset: the first `per_d`
+    instances of each dimension in the seeded config3 draw (d in 2..128,
+    S log-uniform in [257, 65537], n in 2..6, float32 in), forward + VJP
+    (op sum) as one plan per form, each timed as a replayed CUDA graph; plus
+    the per-order error of the mixed form against the plain FP64 form on the
+    same instances (op many; the plain form is pinned to the reference at
+    <= 1e-12 by the test suite)."""
+    from magnus_gb300 import workloads
+    ds, Ss, ns, seeds = workloads.config3_instances(seed=3, count=10000)
+    idx = []
+    for d in (2, 4, 8, 16, 32, 64, 128):
+        idx += [int(i) for i in np.nonzero(ds == d)[0][:per_d]]
+    As, cots, units = [], [], 0
+    for i in idx:
+        d, S = int(ds[i]), int(Ss[i])
+        C, w = workloads.config0_coeffs(int(seeds[i]), d)
+        t = torch.linspace(0.0, 1.0, S, dtype=torch.float64, device=dev)[:, None, None]
+        Ct = torch.as_tensor(C, device=dev)
+        As.append((Ct[0] + Ct[1] * torch.sin(w[0] * t) + Ct[2] * torch.cos(w[1] * t)).to(torch.float32))
+        cots.append(torch.ones((d, d), dtype=torch.float32, device=dev))
+        units += S * int(ns[i])
+
+    def probs(prec, op):
+        return [_lib.make_problem(kind=0, dtype_code=_lib.DTYPE_F32, precision=prec, op=op, integrator=0,
+                                  n=int(ns[i]), samples=int(Ss[i]), dim=int(ds[i]), t0=0.0, tf=1.0) for i in idx]
+
+    res = {}
+    for name, prec in (("mixed", _lib.PRECISION_MIXED), ("plain_fp64", _lib.PRECISION_PLAIN)):
+        outs = [torch.empty((a.shape[1], a.shape[1]), dtype=torch.float32, device=dev) for a in As]
+        dAs = [torch.empty_like(a) for a in As]
+        plan = _plan(lib, _lib, probs(prec, _lib.OP_SUM), As, outs, cots, dAs)
+
+        def step():
+            st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+            _lib.check(lib.mgb_plan_forward(plan, st))
+            _lib.check(lib.mgb_plan_vjp(plan, st))
+
+        ms = _time_graph(torch, step, 2, warmup=1)
+        lib.mgb_plan_destroy(plan)
+        res[name] = {"value": units / (ms / 1e3), "ms": ms, "dA": [g.cpu().numpy() for g in dAs]}
+        # per-order outputs (forward, op many)
+        omany = [torch.empty((int(ns[i]), int(ds[i]), int(ds[i])), dtype=torch.float32, device=dev) for i in idx]
+        pl = _plan(lib, _lib, probs(prec, _lib.OP_MANY), As, omany)
+        _lib.check(lib.mgb_plan_forward(pl, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        torch.cuda.synchronize()
+        lib.mgb_plan_destroy(pl)
+        res[name]["orders"] = [o.cpu().numpy() for o in omany]
+    per_order = [0.0] * 6
+    for om, op_ in zip(res["mixed"]["orders"], res["plain_fp64"]["orders"]):
+        for k, e in enumerate(_order_errors(om.reshape(om.shape[0], -1), op_.reshape(op_.shape[0], -1))):
+            per_order[k] = max(per_order[k], e)
+    e_dA = max(float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+               for a, b in zip(res["mixed"]["dA"], res["plain_fp64"]["dA"]))
+    return {"workload": f"config3 subset: first {per_d} instances of each d in the seeded draw "
+                        f"({len(idx)} instances, {units} samples*order), fwd+VJP, float32",
+            "instances": [{"d": int(ds[i]), "S": int(Ss[i]), "n": int(ns[i])} for i in idx],
+            "mixed": res["mixed"]["value"], "plain_fp64": res["plain_fp64"]["value"],
+            "mixed_over_plain": res["mixed"]["value"] / res["plain_fp64"]["value"],
+            "ms": {"mixed": res["mixed"]["ms"], "plain_fp64": res["plain_fp64"]["ms"]},
+            "rel_err_mixed_vs_fp64_per_order_max": per_order, "rel_err_mixed_vs_fp64_dA_max": e_dA}
+
+
 # ---------------------------------------------------------------- GPU legs
 def main():
     args = parse()
@@ -545,27 +711,19 @@ def main():
     kernels = _lib.profile_read(reset=True)
     launches = sum(v[0] for v in kernels.values()) // args.steps * args.steps
 
-    # ---- roofline of the dominant kernel
-    hbm_peak, bf16_peak, sm_max, peak_src = load_peaks()
-    dom = max(kernels.items(), key=lambda kv: kv[1][1])
-    dom_name, (dom_launches, dom_ms_total) = dom
-    dom_ms = dom_ms_total / dom_launches
-    m = d * d
-    prods = {"chunk_local": (n - 1), "chunk_vjp": 3 * (n - 1)}.get(dom_name, 0)
-    flops = prods * 2.0 * d ** 3 * S * B
-    bytes_alg = {"chunk_local": S * m * 4 * B, "chunk_vjp": 2 * S * m * 4 * B}.get(dom_name, S * m * 4 * B)
-    tflops = flops / (dom_ms / 1e3) / 1e12
-    gbs = bytes_alg / (dom_ms / 1e3) / 1e9
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    if tflops / bf16_peak >= gbs / hbm_peak:
-        roof = {"bound": "tensor", "achieved": tflops, "peak": bf16_peak, "unit": "TFLOP/s", "frac": tflops / bf16_peak}
-    else:
-        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak}
+    # ---- roofline of every timed kernel, and of the dominant one
+    roofs = kernel_roofs(kernels, args.steps, B, S, d, n, c["K"], plain=args.precision == "plain")
+    dom_name = max(roofs, key=lambda k: roofs[k]["ms_per_step"])
+    dom = roofs[dom_name]
     units_scale = (B * S) / (CONFIG4["batch"] * CONFIG4["samples"])
-    roof.update({"kernel": dom_name, "traffic": traffic_from_profiles(dom_name, units_scale), "peak_source": peak_src,
-                 "launch_ms": dom_ms, "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": bytes_alg,
-                 "fp32_simt": {"achieved_tflops": tflops, "nominal_peak_tflops": fp32_peak,
-                               "frac": tflops / fp32_peak}})
+    roof = {"bound": dom["bound"], "achieved": dom["achieved"], "peak": dom["peak"], "unit": dom["unit"],
+            "frac": dom["frac"], "traffic": traffic_from_profiles(dom_name, units_scale), "kernel": dom_name,
+            "peak_source": dom["peak_source"], "launch_ms": dom["launch_ms"],
+            "algorithmic_flops_per_launch": dom["flops_per_launch"],
+            "algorithmic_bytes_per_launch": dom["bytes_per_launch"],
+            "per_kernel": {k: {kk: v[kk] for kk in ("ms_per_step", "bound", "frac", "achieved", "unit", "peak",
+                                                    "peak_source", "compute_frac", "hbm_frac")}
+                           for k, v in roofs.items()}}
 
     result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
               "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -593,16 +751,22 @@ def main():
         def sp(t):
             return (ctypes.c_void_p * sub)(*[t[i].data_ptr() for i in range(sub)])
 
-        # untimed warm-up: the first call of a shape runs the autotuner
-        _lib.check(lib.mgb_forward_batched(probs_p, sub, sp(Ap), sp(out_p), None, sptr))
+        # a plan like the mixed arm's (its creation and autotuning outside
+        # the timed region); one untimed forward + VJP, then one timed
+        plan_p = ctypes.c_void_p()
+        _lib.check(lib.mgb_plan_create(probs_p, sub, sp(Ap), sp(out_p), sp(cot[:sub]), sp(dA_p),
+                                       ctypes.byref(plan_p)))
+        _lib.check(lib.mgb_plan_forward(plan_p, sptr))
+        _lib.check(lib.mgb_plan_vjp(plan_p, sptr))
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
         f0.record(stream)
-        _lib.check(lib.mgb_forward_batched(probs_p, sub, sp(Ap), sp(out_p), None, sptr))
-        _lib.check(lib.mgb_vjp_batched(probs_p, sub, sp(Ap), sp(cot[:sub]), None, sp(dA_p), sptr))
+        _lib.check(lib.mgb_plan_forward(plan_p, sptr))
+        _lib.check(lib.mgb_plan_vjp(plan_p, sptr))
         f1.record(stream)
         torch.cuda.synchronize()
+        _lib.check(lib.mgb_plan_destroy(plan_p))
         plain_ms = f0.elapsed_time(f1)
         plain_value = sub * S * n / (plain_ms / 1e3)
         # mixed (already computed in the timed steps for these instances) vs FP64
@@ -612,6 +776,13 @@ def main():
                                 "mixed_speedup": value / world / plain_value}
         result["rel_err_mixed_vs_fp64"] = {"out": e_out, "dA": e_dA, "instances": sub}
         del out_p, dA_p
+        # the timed steps' outputs of the first instances, for the check
+        # against the FP64 oracle in the CPU leg below
+        nck = min(args.oracle_instances, B)
+        ck_in = (A[:nck].cpu().numpy(), cot[:nck].cpu().numpy(), out[:nck].cpu().numpy(), dA[:nck].cpu().numpy())
+
+        # ---- config3's mixed-over-plain target on a fixed subset
+        result["config3_subset"] = config3_subset(torch, lib, _lib, dev)
 
         # ---- end to end through the public autograd API, pinned host buffers
         eb = min(args.e2e_batch, B)
@@ -692,6 +863,8 @@ def main():
         result["cpu_baseline"] = {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": f"{inst} config4 trajectories at S={args.cpu_samples} (of 32769), "
                                             f"fwd + VJP, float32, {cpu_s:.1f} s", "cpu_model": cpu_model()}
+        if nck:
+            result["rel_err_mixed_vs_oracle"] = oracle_check(*ck_in, n=n, t0=c["t0"], tf=c["tf"])
     if plan is not None and plan.value:
         _lib.check(lib.mgb_plan_destroy(plan))
     if rank == 0:

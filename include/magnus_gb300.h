@@ -186,6 +186,16 @@ size_t mgb_max_order(void);
  * device entry points and plans check it when they synchronize. */
 mgb_status mgb_device_check(void);
 
+/* Engine-specific, no reference counterpart: a self-test of the error path
+ * above.  Enqueues one small kernel that waits up to limit_ns (at most 2e9)
+ * on a device-side barrier nothing arrives at, then gives up the way the
+ * engine's kernels do (raises the time-out flag and returns; nothing else is
+ * in flight).  The next mgb_device_check() returns MGB_ERR_DEVICE_TIMEOUT and
+ * clears the flag; the context stays usable.  Mirrors the error contract of
+ * the reference's JAX handlers (src/api/jax_ffi.cpp:280-284): a failure is a
+ * status, not an abort. */
+mgb_status mgb_selftest_bounded_wait(int64_t limit_ns, void* stream);
+
 /* Kernel timing.  While enabled, every engine kernel launch is bracketed by
  * CUDA events on its stream; mgb_profile_read waits for the recorded events,
  * fills up to `capacity` entries (one per kernel name: launches and total

@@ -267,6 +267,8 @@ struct Call {
 // a CUDA graph).  This is the engine's counterpart of the reference's
 // KernelPlan made by make_plan / make_vjp_plan
 // (src/composer/dispatch.hpp:446-492, src/composer/backends.cpp:65-102).
+int env_int(const char* name, int dflt);
+
 struct Segment {
     int32_t first = 0, count = 0;  // instance range (sorted order)
     int64_t work_off = 0, nwork = 0;
@@ -277,6 +279,8 @@ struct Segment {
     // chunk scans spread over the GPU (matrix, d a multiple of 16):
     // active[c] = instances of the segment with more than c chunks
     bool tiled_scan = false;
+    // mixed form at d = 16 / 32: both scans in one double-FP32 launch each
+    bool df_scan = false;
     int d = 0, nmax = 0;
     std::vector<int32_t> active;
     // chunk-kernel launch variant (autotuner) and the times it measured
@@ -408,6 +412,7 @@ mgb_status plan_layout(const Call& call, PlanCore& pc, std::vector<Derived>& dv)
         }
         sg.d = sg.hi[0].d;
         sg.tiled_scan = scan_tiled_ok(pc.kind, sg.d);
+        sg.df_scan = sg.tiled_scan && !pc.plain && env_int("MGB_DF_SCAN", 1) != 0 && scan_df_ok(pc.kind, sg.d, sg.nmax);
         if (sg.tiled_scan) {
             sg.active.assign((size_t)dv[pc.order[a]].C, 0);
             for (size_t k = a; k < b; ++k)
@@ -544,10 +549,14 @@ mgb_status plan_upload(PlanCore& pc, cudaStream_t st, bool synchronous) {
 }
 
 mgb_status plan_streams(PlanCore& pc) {
-    for (const Segment& sg : pc.segs)
+    for (const Segment& sg : pc.segs) {
         for (int mode : {MODE_LOCAL, MODE_VJP})
             MGB_CUDA_TRY(prepare_tuned(choose_tuned(pc.plain, pc.kind, pc.rule, mode, pc.f64io != 0, sg.hi, sg.variant),
                                        pc.rule, mode));
+        if (sg.df_scan)
+            for (bool rev : {false, true})
+                MGB_CUDA_TRY(launch_scan_df(nullptr, 0, sg.d, sg.nmax, rev, pc.f64io, nullptr, true));
+    }
     if (pc.segs.size() < 2 || pc.fork) return MGB_OK;
     MGB_CUDA_TRY(cudaEventCreateWithFlags(&pc.fork, cudaEventDisableTiming));
     for (Segment& sg : pc.segs) {
@@ -721,7 +730,9 @@ int64_t seg_nm(const Segment& sg) { return (int64_t)sg.nmax * sg.d * sg.d; }
 // Forward scan over a segment's chunks: pi^0..pi^C.
 mgb_status seg_scan(PlanCore& pc, Segment& sg, cudaStream_t s) {
     const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
-    if (sg.tiled_scan)
+    if (sg.df_scan)
+        MGB_CUDA_TRY(timed("scan", s, [&] { return launch_scan_df(di, sg.count, sg.d, sg.nmax, false, pc.f64io, s); }));
+    else if (sg.tiled_scan)
         MGB_CUDA_TRY(timed("scan", s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, false, pc.f64io, s); }));
     else
         MGB_CUDA_TRY(timed("scan", s, [&] { return launch_small(true, pc.kind, SMALL_SCAN, di, sg.count, pc.f64io, 0, seg_nm(sg), s); }));
@@ -730,7 +741,9 @@ mgb_status seg_scan(PlanCore& pc, Segment& sg, cudaStream_t s) {
 
 mgb_status seg_small(PlanCore& pc, Segment& sg, int which, int write_out, cudaStream_t s, const char* name) {
     const InstDev* di = reinterpret_cast<const InstDev*>(pc.base + pc.off_inst) + sg.first;
-    if (which == SMALL_RSCAN && sg.tiled_scan)
+    if (which == SMALL_RSCAN && sg.df_scan)
+        MGB_CUDA_TRY(timed(name, s, [&] { return launch_scan_df(di, sg.count, sg.d, sg.nmax, true, pc.f64io, s); }));
+    else if (which == SMALL_RSCAN && sg.tiled_scan)
         MGB_CUDA_TRY(timed(name, s, [&] { return launch_scan_tiled(di, sg.count, sg.d, sg.nmax, sg.active, true, pc.f64io, s); }));
     else if ((which == SMALL_FIN_FWD || which == SMALL_FIN_VJP) && sg.tiled_scan)
         MGB_CUDA_TRY(timed(name, s, [&] {
@@ -1036,7 +1049,11 @@ size_t mgb_plan_describe(const mgb_plan* plan, char* buf, size_t len) {
     for (size_t i = 0; i < pc.segs.size(); ++i) {
         const Segment& sg = pc.segs[i];
         const TunedChoice tc = choose_tuned(pc.plain, pc.kind, pc.rule, MODE_LOCAL, pc.f64io != 0, sg.hi, sg.variant);
-        const char* kernel = !tc.use ? "k_chunk" : tc.family == 1 ? "k_small" : tc.family == 2 ? "k_tile" : "k_bigtc";
+        // the forward local pass's kernel; at d = 32 variants 2 and 3 run the
+        // VJP on the warp-MMA kernel
+        const char* kernel = !tc.use ? "k_chunk" : tc.family == 1 ? "k_small" : tc.family == 3 ? "k_bigtc"
+                             : (tc.D == 32 && sg.variant == 2) ? "k_tiletc"
+                             : (tc.D == 32 && sg.variant == 3) ? "k_mma32" : "k_tile";
         const int ctas = !tc.use ? generic_ctas_per_sm(sg.variant % GENERIC_VARIANTS) : tc.ctas_per_sm;
         std::snprintf(tmp, sizeof(tmp),
                       "%s{\"d\": %d, \"instances\": %d, \"chunks\": %lld, \"kernel\": \"%s\", \"variant\": %d, "
@@ -1434,6 +1451,14 @@ mgb_status mgb_device_check(void) {
     const cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return fail(MGB_ERR_CUDA, cudaGetErrorString(e));
     if (read_clear_device_timeout()) return fail(MGB_ERR_DEVICE_TIMEOUT, "a device-side wait timed out");
+    return MGB_OK;
+}
+
+mgb_status mgb_selftest_bounded_wait(int64_t limit_ns, void* stream) {
+    g_last_error.clear();
+    if (limit_ns <= 0 || limit_ns > 2000000000LL)
+        return fail(MGB_ERR_INVALID_ARGUMENT, "limit_ns must be in (0, 2e9]");
+    MGB_CUDA_TRY(launch_wait_selftest((uint64_t)limit_ns, static_cast<cudaStream_t>(stream)));
     return MGB_OK;
 }
 

@@ -59,6 +59,12 @@ cudaError_t launch_fin_tiled(const InstDev* insts, int count, int d, int nmax, b
                              cudaStream_t st);
 
 bool scan_tiled_ok(int kind, int d);
+// Mixed-form chunk scans in double-FP32 arithmetic, one CTA per instance and
+// one launch per direction (mgb_scan_df.cu), for d = 16 / 32 matrices whose
+// state and transfers (4 n d^2 floats) fit in 200 KB of shared memory.
+bool scan_df_ok(int kind, int d, int nmax);
+cudaError_t launch_scan_df(const InstDev* insts, int count, int d, int nmax, bool reverse, int f64io,
+                           cudaStream_t st, bool prepare_only = false);
 cudaError_t launch_scan_tiled(const InstDev* insts, int count, int d, int nmax, const std::vector<int32_t>& active,
                               bool reverse, int f64io, cudaStream_t st);
 

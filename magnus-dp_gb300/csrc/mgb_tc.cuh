@@ -42,15 +42,20 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// Wait for the phase of the given parity; false after ~2 s.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+// Wait for the phase of the given parity; false after limit_ns of
+// %globaltimer.
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
     if (mbar_try(mbar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
         for (int i = 0; i < 64; ++i)
             if (mbar_try(mbar, parity)) return true;
-        if (global_ns() - t0 > 2000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
+}
+// The kernels' bounded wait: false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    return mbar_wait_ns(mbar, parity, 2000000000ull);
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

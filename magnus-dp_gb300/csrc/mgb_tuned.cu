@@ -487,13 +487,15 @@ cudaError_t launch_tile_m(int rule, int mode, const LaunchArgs& a, int grid, boo
 
 }  // namespace
 
-// variant 0: two CTAs per SM (if shared memory allows), 1: one, 2 (d = 32):
-// the tensor-core forward local pass (the VJP then runs variant 0)
+// variant 0: two CTAs per SM (if shared memory allows), 1: one; at d = 32
+// variant 2: the tcgen05 forward local pass with the warp-MMA VJP, 3: the
+// warp-MMA kernel (mgb_mma32.cu) for both
 cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only) {
-    if (variant == 2) {
-        if (D == 32 && mode == MODE_LOCAL) return launch_tiletc(rule, a, grid, prepare_only);
-        variant = 0;
+    if (D == 32 && variant >= 2) {
+        if (variant == 2 && mode == MODE_LOCAL) return launch_tiletc(rule, a, grid, prepare_only);
+        return launch_mma32(rule, mode, a, grid, prepare_only);
     }
+    if (variant >= 2) variant = 0;
     if (D == 32) return variant == 0 ? launch_tile_m<32, 2>(rule, mode, a, grid, prepare_only)
                                      : launch_tile_m<32, 1>(rule, mode, a, grid, prepare_only);
     return variant == 0 ? launch_tile_m<16, 2>(rule, mode, a, grid, prepare_only)
@@ -544,7 +546,7 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     tc.family = 2;
     tc.D = D;
     tc.nmax = nmax;
-    tc.nvariants = smem <= 113 * 1024 ? (D == 32 ? 3 : 2) : 1;
+    tc.nvariants = smem <= 113 * 1024 ? (D == 32 ? 4 : 2) : 1;
     tc.variant = variant < tc.nvariants ? variant : 0;
     if (tc.nvariants == 1) tc.variant = 1;  // one CTA per SM only
     tc.ctas_per_sm = tc.variant == 1 ? 1 : 2;

@@ -39,12 +39,18 @@ cudaError_t launch_big(int D, int rule, int mode, const LaunchArgs& a, int sms, 
 int big_variants(int D);
 int big_ctas_per_sm(int D, int variant);
 // Group-tiled kernel (mgb_tuned.cu), variant 0: 2 CTAs per SM, 1: one;
-// variant 2 (d = 32): the forward local pass on the tensor cores
-// (mgb_tiletc.cu; the VJP then takes variant 0).
+// at d = 32 variant 2: the tcgen05 forward local pass (mgb_tiletc.cu) with
+// the warp-MMA VJP, variant 3: the warp-MMA kernel for both.
 cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only);
 cudaError_t launch_tiletc(int rule, const LaunchArgs& a, int grid, bool prepare_only);
+// Warp-MMA kernel at d = 32 (mgb_mma32.cu), forward local pass and VJP; two
+// CTAs per SM.
+cudaError_t launch_mma32(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only);
 // Device address of the time-out flag the tensor-core kernels raise.
 int* device_timeout_ptr();
+// One CTA waits (limit_ns) on an mbarrier nothing arrives at and raises the
+// time-out flag (mgb_selftest.cu).
+cudaError_t launch_wait_selftest(uint64_t limit_ns, cudaStream_t st);
 // Generic kernel variants: 8, 4 or 2 CTAs per SM.
 constexpr int GENERIC_VARIANTS = 3;
 int generic_ctas_per_sm(int variant);

@@ -63,6 +63,7 @@ SIGNATURES = {
     "mgb_set_gl_table": (ctypes.c_int, [ctypes.c_size_t, _VP, _VP]),
     "mgb_max_order": (ctypes.c_size_t, []),
     "mgb_device_check": (ctypes.c_int, []),
+    "mgb_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int64, _VP]),
     "mgb_last_error": (ctypes.c_char_p, []),
     "mgb_version": (ctypes.c_int, []),
     "mgb_forward_noalloc": (ctypes.c_int, [_PP, _VP, _VP, _VP]),

@@ -57,21 +57,23 @@ RULES = {0: "Boole", 1: "Simpson", 2: "Trapezoid", 3: "Riemann"}
 
 
 @pytest.mark.parametrize("d,nvariants,precision,dtype_name,tol,kernel", [
-    (32, 3, _lib.PRECISION_MIXED, "float32", 1e-6, "k_tile"),  # 2: tensor-core forward
+    # 2: tcgen05 forward + warp-MMA VJP, 3: warp-MMA forward and VJP
+    (32, 4, _lib.PRECISION_MIXED, "float32", 1e-6, ["k_tile", "k_tile", "k_tiletc", "k_mma32"]),
     (16, 2, _lib.PRECISION_MIXED, "float32", 1e-6, "k_tile"),
     (64, 5, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),  # 4: one accumulator pair, 3 CTAs/SM
     (128, 3, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),  # 2: one accumulator pair, 2 CTAs/SM
     (8, 3, _lib.PRECISION_PLAIN, "float64", 1e-12, "k_chunk"),
 ])
-@pytest.mark.parametrize("integrator", [0, 1])
+@pytest.mark.parametrize("integrator", [0, 1, 2, 3])
 def test_every_variant_matches_oracle(d, nvariants, precision, dtype_name, tol, kernel, integrator, cuda, monkeypatch):
-    S = 129 if integrator == 0 else 131
+    S = {0: 129, 1: 131, 2: 97, 3: 90}[integrator]
     specs = [(d, S, 4), (d, 2 * S - 1, 3)]
     for v in range(nvariants):
         monkeypatch.setenv("MGB_FORCE_VARIANT", str(v))
         host, outs, dAs, desc = _run_plan(cuda, specs, precision, dtype_name, integrator=integrator)
         seg = desc["segments"][0]
-        assert seg["kernel"] == kernel and seg["variant"] == v, seg
+        want = kernel[v] if isinstance(kernel, list) else kernel
+        assert seg["kernel"] == want and seg["variant"] == v, seg
         for (A, cot, n), o, g in zip(host, outs, dAs):
             A64 = A.astype(np.float64)
             ref = O.forward(A64, n, 0.0, 1.0, "sum", RULES[integrator])
@@ -86,8 +88,8 @@ def test_plan_reports_tuned_variant(cuda, monkeypatch):
     specs = [(32, 1025, 5)] * 4 + [(64, 513, 4)] * 2
     host, outs, dAs, desc = _run_plan(cuda, specs, _lib.PRECISION_MIXED, "float32", K=64)
     by_d = {s["d"]: s for s in desc["segments"]}
-    assert by_d[32]["kernel"] == "k_tile" and by_d[64]["kernel"] == "k_bigtc"
-    for seg, nv in ((by_d[32], 3), (by_d[64], 5)):
+    assert by_d[32]["kernel"] in ("k_tile", "k_tiletc", "k_mma32") and by_d[64]["kernel"] == "k_bigtc"
+    for seg, nv in ((by_d[32], 4), (by_d[64], 5)):
         ms = seg["tuned_ms"]
         assert len(ms) == nv and all(t > 0 for t in ms), seg
         assert ms[seg["variant"]] == min(ms), seg  # the fastest (ties: either)
