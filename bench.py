@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--samples", type=int, default=CONFIG4["samples"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--plain-subset", type=int, default=16)
-    ap.add_argument("--e2e-batch", type=int, default=128)
+    ap.add_argument("--e2e-batch", type=int, default=0,
+                    help="instances of the end-to-end legs (0: the whole batch, if host memory allows)")
     ap.add_argument("--cpu-instances", type=int, default=0, help="0 = one per host thread")
     ap.add_argument("--cpu-samples", type=int, default=4097)
     ap.add_argument("--oracle-instances", type=int, default=4,
@@ -193,6 +194,23 @@ def oracle_check(A, cot, out, dA, n, t0, tf):
     e_dA = float(np.linalg.norm(dA.astype(np.float64) - rg) / np.linalg.norm(rg))
     return {"out": e_out, "dA": e_dA, "instances": len(jobs), "checker": "oracle/collapsed.py (FP64)",
             "seconds": time.perf_counter() - t}
+
+
+def e2e_instances(B, bytes_per_instance):
+    """Instances for the end-to-end legs: the whole batch when page-locked
+    host buffers for its input and dA (two copies) fit in half of the host's
+    available memory, else as many as do."""
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    if avail is None:
+        return min(B, 128)
+    return max(1, min(B, int(0.5 * avail // (2 * bytes_per_instance))))
 
 
 def cpu_model():
@@ -785,7 +803,7 @@ def main():
         result["config3_subset"] = config3_subset(torch, lib, _lib, dev)
 
         # ---- end to end through the public autograd API, pinned host buffers
-        eb = min(args.e2e_batch, B)
+        eb = min(args.e2e_batch, B) if args.e2e_batch > 0 else e2e_instances(B, S * d * d * 4)
         A_host = torch.empty((eb, S, d, d), dtype=torch.float32, pin_memory=True)
         A_host.copy_(A[:eb])
         cot_host = cot[:eb].cpu().pin_memory()
@@ -850,11 +868,26 @@ def main():
             host_step()
             host_ms_all.append((time.perf_counter() - t0h) * 1e3)
         host_ms = statistics.median(host_ms_all)
+        # one more call with the library's launch timing on: per-stage device
+        # time (copies in, kernels, copies out) against the wall clock, to
+        # show how far the stages overlap
+        lib.mgb_profile_enable(1)
+        _lib.profile_read(reset=True)
+        t0h = time.perf_counter()
+        host_step()
+        prof_wall = (time.perf_counter() - t0h) * 1e3
+        lib.mgb_profile_enable(0)
+        stages = _lib.profile_read(reset=True)
+        stage_ms = {"h2d": stages.get("h2d", (0, 0.0))[1], "d2h": stages.get("d2h", (0, 0.0))[1],
+                    "kernels": sum(v[1] for k, v in stages.items() if k not in ("h2d", "d2h")), "wall": prof_wall}
         result["e2e"] = {"value": eb * S * n / (host_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "instances": eb, "ms_per_step": host_ms,
                          "ms_per_step_min_max": [min(host_ms_all), max(host_ms_all)], "steps": len(host_ms_all),
                          "api": "mgb_fwd_vjp_host_batched (C ABI, host buffers, synchronous; wall clock, median "
-                                "of 5 calls: host-to-device copy rates on this machine vary between calls)"}
+                                "of 5 calls: host-to-device copy rates on this machine vary between calls)",
+                         "stage_ms_one_call": stage_ms,
+                         "link_gbs": {"h2d": h2d / (stage_ms["h2d"] / 1e3) / 1e9 if stage_ms["h2d"] else None,
+                                      "d2h": d2h / (stage_ms["d2h"] / 1e3) / 1e9 if stage_ms["d2h"] else None}}
 
         # ---- CPU baseline (oracle port on the host cores, bounded sample)
         threads = os.cpu_count() or 1

@@ -1053,7 +1053,8 @@ size_t mgb_plan_describe(const mgb_plan* plan, char* buf, size_t len) {
         // VJP on the warp-MMA kernel
         const char* kernel = !tc.use ? "k_chunk" : tc.family == 1 ? "k_small" : tc.family == 3 ? "k_bigtc"
                              : (tc.D == 32 && sg.variant == 2) ? "k_tiletc"
-                             : (tc.D == 32 && sg.variant == 3) ? "k_mma32" : "k_tile";
+                             : (tc.D == 32 && sg.variant == 3) ? "k_mma32"
+                             : (tc.D == 32 && sg.variant == 4) ? "k_mma32t" : "k_tile";
         const int ctas = !tc.use ? generic_ctas_per_sm(sg.variant % GENERIC_VARIANTS) : tc.ctas_per_sm;
         std::snprintf(tmp, sizeof(tmp),
                       "%s{\"d\": %d, \"instances\": %d, \"chunks\": %lld, \"kernel\": \"%s\", \"variant\": %d, "
@@ -1389,10 +1390,15 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
         if (st == MGB_OK) st = plan_streams(u.pc);
         if (st != MGB_OK) break;
         if (used[k]) e = cudaStreamWaitEvent(sin, ev_out[k], 0);
-        for (size_t j = 0; j < cnt && e == cudaSuccess; ++j) {
-            e = stage_copy(const_cast<void*>(u.in[j]), A[i0 + j], bin[i0 + j], true, sms, sin);
-            if (e == cudaSuccess) e = stage_copy(const_cast<void*>(u.cot[j]), cot[i0 + j], bout[i0 + j], true, sms, sin);
-        }
+        if (e == cudaSuccess)
+            e = timed("h2d", sin, [&] {
+                cudaError_t r = cudaSuccess;
+                for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
+                    r = stage_copy(const_cast<void*>(u.in[j]), A[i0 + j], bin[i0 + j], true, sms, sin);
+                    if (r == cudaSuccess) r = stage_copy(const_cast<void*>(u.cot[j]), cot[i0 + j], bout[i0 + j], true, sms, sin);
+                }
+                return r;
+            });
         if (e == cudaSuccess) e = cudaEventRecord(ev_in[k], sin);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(scomp, ev_in[k], 0);
         if (e != cudaSuccess) {
@@ -1404,10 +1410,15 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
         if (st != MGB_OK) break;
         e = cudaEventRecord(ev_comp[k], scomp);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sout, ev_comp[k], 0);
-        for (size_t j = 0; j < cnt && e == cudaSuccess; ++j) {
-            e = stage_copy(out[i0 + j], u.out[j], bout[i0 + j], false, sms, sout);
-            if (e == cudaSuccess) e = stage_copy(dA[i0 + j], u.dA[j], bin[i0 + j], false, sms, sout);
-        }
+        if (e == cudaSuccess)
+            e = timed("d2h", sout, [&] {
+                cudaError_t r = cudaSuccess;
+                for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
+                    r = stage_copy(out[i0 + j], u.out[j], bout[i0 + j], false, sms, sout);
+                    if (r == cudaSuccess) r = stage_copy(dA[i0 + j], u.dA[j], bin[i0 + j], false, sms, sout);
+                }
+                return r;
+            });
         if (e == cudaSuccess) e = cudaEventRecord(ev_out[k], sout);
         if (e != cudaSuccess) st = cuda_fail(e);
         used[k] = true;

@@ -17,19 +17,28 @@
 // accumulation step): measured 4.7e-8 relative per 32^3 product, against
 // 1.0e-7 for FP32 FMA (3.2e-7 with a single accumulator).
 //
-// Layout (one CTA of NW = 4 warps per chunk, samples in groups of G = 4 = a
-// Boole block; warp s owns sample s of the group in the product phases):
-//   xa  A of the group as BF16 pieces             [G][3][32 x 32], swizzled
+// Layout (one CTA of NW = 8 warps per chunk, samples in groups of G = 4 = a
+// Boole block; in the product phases warps 2s and 2s + 1 own sample s, each
+// one 32 x 16 column half of it, so that sixteen warps per SM (two CTAs)
+// hide the latency of the prefix and split work):
+//   xa  A as BF16 pieces, five sample slots        [5][3][32 x 32], swizzled
 //   xb  P_j (forward) or G_{j+1} (adjoint) pieces [G][3][32 x 32]
-//   xc  P_j from the replay tape (adjoint)         [G][3][32 x 32]
-//   sw  FP32 product outputs (prefix input)        [G][32][40]
-//   sg  FP32 staging of a bulk copy (A of a group or a tape level)
+//   xc  P_j of the group (adjoint)                 [G][3][32 x 32]
+//   sw  FP32 product outputs (prefix input)        [G][32][36]
+//   sg  FP32 staging of a bulk copy (A of a group's samples or one level of
+//       the group's P buffer)
 // Piece tiles hold 64-byte rows with the 16-byte chunk c stored at c ^
 // ((row >> 1) & 3): ldmatrix of 8 rows and the prefix threads' row stores are
 // both free of bank conflicts.
 //
-// A of each group and (adjoint) each tape level arrive by TMA bulk copies
-// (cp.async.bulk, completion on an mbarrier), one copy ahead of their use.
+// A of each group and (adjoint) each level of the group's P buffer arrive by
+// TMA bulk copies (cp.async.bulk, completion on an mbarrier), one copy ahead
+// of their use.  The adjoint needs every P_j at every sample in reverse
+// order; instead of replaying the chunk forward into a chunk-long tape (4 KB
+// per sample and level through HBM, twice), each group's P_j are rebuilt
+// backwards from the group end (the chunk end holds P_j = pi^{c+1}_j) by the
+// inverse block rules on compensated FP32 pairs, with W_j = A P_{j-1}
+// recomputed on the tensor cores.
 // Prefix passes are the shared block-rule state machines (fwd_step /
 // rev_step) with FP32 compensated local accumulators and the FP64 chunk
 // carries added as hi + lo, per-level state in the CTA's global slot as in
@@ -38,112 +47,62 @@
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "mgb_common.cuh"
+#include "mgb_mma.cuh"
 #include "mgb_tc.cuh"
 #include "mgb_tuned.h"
 
 namespace mgb {
 namespace {
 
+using namespace wm;
+
 constexpr int D = 32, m = D * D;
-constexpr int NW = 4, NT = 32 * NW, G = NW;
-constexpr int NP = m / 2 / NT;        // element pairs per thread per sample (4)
-constexpr int WP = 40;                // FP32 row pitch of sw (conflict-free float2 epilogue stores)
-constexpr uint32_t PT = 32 * 64;      // bytes per piece tile (32 rows x 64 B)
+constexpr int NW = 8, NT = 32 * NW, G = 4;
+constexpr int NP = m / 2 / NT;        // element pairs per thread per sample (2)
+constexpr int WP = 36;                // FP32 row pitch of sw
 constexpr uint32_t SX = G * 3 * PT;   // bytes per operand set
-constexpr size_t OFF_XA = 0, OFF_XB = SX, OFF_XC = 2 * (size_t)SX, OFF_W = 3 * (size_t)SX;
+// xa holds five sample sets: the VJP keeps A of a group's anchor and of its
+// four samples (a ring indexed by sample % 5)
+constexpr size_t OFF_XA = 0, OFF_XB = 5 * 3 * (size_t)PT, OFF_XC = OFF_XB + SX, OFF_W = OFF_XC + SX;
 constexpr size_t OFF_SG = OFF_W + (size_t)G * 32 * WP * 4;
 constexpr size_t OFF_BAR = OFF_SG + (size_t)G * m * 4;
 constexpr size_t SMEM = OFF_BAR + 64;
 static_assert(NP * 2 * NT == m, "pair mapping");
+static_assert(SMEM + 1024 <= 114 * 1024, "two CTAs per SM");
 
-// byte offset of (row, col) in a piece tile; col a multiple of 8 for ldmatrix rows
-__device__ __forceinline__ uint32_t toff(int r, int c) {
-    return (uint32_t)r * 64u + ((uint32_t)((c >> 3) ^ ((r >> 1) & 3)) << 4) + (uint32_t)(c & 7) * 2u;
-}
-
-__device__ __forceinline__ void ldsm4(uint32_t a, uint32_t (&r)[4]) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-__device__ __forceinline__ void ldsm4t(uint32_t a, uint32_t (&r)[4]) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-__device__ __forceinline__ void mma16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// Exact three-piece BF16 split of two values, packed per piece (low half =
-// the first value).
-__device__ __forceinline__ void split2(float x, float y, uint32_t& p0, uint32_t& p1, uint32_t& p2) {
-    const __nv_bfloat162 b0 = __floats2bfloat162_rn(x, y);
-    const float2 f0 = __bfloat1622float2(b0);
-    const float rx = x - f0.x, ry = y - f0.y;
-    const __nv_bfloat162 b1 = __floats2bfloat162_rn(rx, ry);
-    const float2 f1 = __bfloat1622float2(b1);
-    const __nv_bfloat162 b2 = __floats2bfloat162_rn(rx - f1.x, ry - f1.y);
-    p0 = *reinterpret_cast<const uint32_t*>(&b0);
-    p1 = *reinterpret_cast<const uint32_t*>(&b1);
-    p2 = *reinterpret_cast<const uint32_t*>(&b2);
-}
-
-// Store a pair (row r, columns c, c+1) of FP32 values as pieces of tile set t.
-__device__ __forceinline__ void put_pair(uint8_t* t, int r, int c, float x, float y) {
-    uint32_t p0, p1, p2;
-    split2(x, y, p0, p1, p2);
-    const uint32_t o = toff(r, c);
-    *reinterpret_cast<uint32_t*>(t + o) = p0;
-    *reinterpret_cast<uint32_t*>(t + PT + o) = p1;
-    *reinterpret_cast<uint32_t*>(t + 2 * PT + o) = p2;
-}
-
-// Store four consecutive FP32 values (row r, columns c..c+3, c % 4 == 0).
-__device__ __forceinline__ void put_quad(uint8_t* t, int r, int c, float4 v) {
-    uint32_t a0, a1, a2, b0, b1, b2;
-    split2(v.x, v.y, a0, a1, a2);
-    split2(v.z, v.w, b0, b1, b2);
-    const uint32_t o = toff(r, c);
-    *reinterpret_cast<uint2*>(t + o) = make_uint2(a0, b0);
-    *reinterpret_cast<uint2*>(t + PT + o) = make_uint2(a1, b1);
-    *reinterpret_cast<uint2*>(t + 2 * PT + o) = make_uint2(a2, b2);
-}
-
-// One warp: acc (main, small) [mt][nt] += X Y for one sample, X and Y 32 x 32
-// given as BF16 piece tiles (3 tiles, PT bytes apart) in row-major storage S:
+// One warp: acc (main, small) [mt][nt] += (X Y)[:, 16 nh .. 16 nh + 15] for
+// one sample, X and Y 32 x 32 given as BF16 piece tiles (3 tiles, PT bytes
+// apart) in row-major storage S:
 //   XT = false: X = S_x (rows m, cols k);  XT = true: X = S_x^T
 //   YT = false: Y = S_y (rows k, cols n);  YT = true: Y = S_y^T
-// The MMAs are issued piece pair by piece pair over all eight output tiles,
+// The MMAs are issued piece pair by piece pair over the four output tiles,
 // so that consecutive MMAs never feed the same accumulator (an accumulator's
 // next MMA waits out the previous one's latency).
 template <bool XT, bool YT>
-__device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&am)[2][4][4], float (&as)[2][4][4],
-                                             int lane) {
+__device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&am)[2][2][4], float (&as)[2][2][4],
+                                             int lane, int nh) {
     const int l8 = lane & 7, lb = (lane >> 3) & 1, lh = lane >> 4;
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
-        uint32_t bf[3][4][2];  // [piece][n-tile][reg]
+        uint32_t bf[3][2][2];  // [piece][n-tile][reg]
         uint32_t af[3][2][4];  // [piece][m-tile][reg]
-#pragma unroll
-        for (int ntp = 0; ntp < 2; ++ntp) {
+        {
             uint32_t o;
-            if (!YT) o = toff(ks * 16 + l8 + 8 * lb, (2 * ntp + lh) * 8);   // trans: rows k, cols n
-            else o = toff((2 * ntp + lh) * 8 + l8, ks * 16 + 8 * lb);        // rows n, cols k
+            if (!YT) o = toff(ks * 16 + l8 + 8 * lb, (2 * nh + lh) * 8);   // trans: rows k, cols n
+            else o = toff((2 * nh + lh) * 8 + l8, ks * 16 + 8 * lb);        // rows n, cols k
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 uint32_t r[4];
                 if (!YT) ldsm4t(ys + p * PT + o, r);
                 else ldsm4(ys + p * PT + o, r);
-                bf[p][2 * ntp][0] = r[0];
-                bf[p][2 * ntp][1] = r[1];
-                bf[p][2 * ntp + 1][0] = r[2];
-                bf[p][2 * ntp + 1][1] = r[3];
+                bf[p][0][0] = r[0];
+                bf[p][0][1] = r[1];
+                bf[p][1][0] = r[2];
+                bf[p][1][1] = r[3];
             }
         }
 #pragma unroll
@@ -164,44 +123,33 @@ __device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&a
 #pragma unroll
             for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                for (int nt = 0; nt < 4; ++nt)
+                for (int nt = 0; nt < 2; ++nt)
                     mma16816(q == 5 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0], bf[PJ[q]][nt][1]);
     }
 }
 
-__device__ __forceinline__ void zero_acc(float (&a)[2][4][4]) {
+__device__ __forceinline__ void zero_acc(float (&a)[2][2][4]) {
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 2; ++j)
 #pragma unroll
             for (int k = 0; k < 4; ++k) a[i][j][k] = 0.f;
 }
 
-// FP32 output tile of one warp's product (main + small) into sw (pitch WP)
-__device__ __forceinline__ void store_acc(float* o, const float (&am)[2][4][4], const float (&as)[2][4][4], int g8,
-                                          int t4) {
+// FP32 output half-tile of one warp's product (main + small) into sw (pitch WP)
+__device__ __forceinline__ void store_acc(float* o, const float (&am)[2][2][4], const float (&as)[2][2][4], int g8,
+                                          int t4, int nh) {
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const int r = mt * 16 + g8, cc = nt * 8 + 2 * t4;
+        for (int nt = 0; nt < 2; ++nt) {
+            const int r = mt * 16 + g8, cc = (2 * nh + nt) * 8 + 2 * t4;
             *reinterpret_cast<float2*>(o + r * WP + cc) =
                 make_float2(am[mt][nt][0] + as[mt][nt][0], am[mt][nt][1] + as[mt][nt][1]);
             *reinterpret_cast<float2*>(o + (r + 8) * WP + cc) =
                 make_float2(am[mt][nt][2] + as[mt][nt][2], am[mt][nt][3] + as[mt][nt][3]);
         }
-}
-
-// Bulk copy of `bytes` (a multiple of 16) from global to shared memory,
-// completing on the mbarrier.
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    const uint32_t b = tc::su32(bar);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(tc::su32(dst)),
-        "l"(src), "r"(bytes), "r"(b)
-        : "memory");
 }
 
 template <int RULE, int MODE>
@@ -217,6 +165,7 @@ __global__ void __launch_bounds__(NT, 2)
     uint64_t* const bar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g8 = lane >> 2, t4 = lane & 3;
+    const int ws = warp >> 1, nh = warp & 1;  // product phases: sample ws, column half nh
     const uint32_t sxa = tc::su32(xa), sxb = tc::su32(xb), sxc = tc::su32(xc);
 
     if (tid == 0) {
@@ -252,15 +201,21 @@ __global__ void __launch_bounds__(NT, 2)
         const RuleCoef<float> kc = rule_coef<float>(I);
         const double* pic = I.pi + (int64_t)c * nm;
         const float* Ag = static_cast<const float*>(I.A) + b * m;
-        const int NLf = (MODE == MODE_LOCAL) ? n : n - 1;
-        float* const st = slot;                              // [n][3][m] prefix state
-        float* const tape = slot + (int64_t)3 * n * m;       // [n-1][L][m]
-        float* const cyt = tape + (int64_t)(n - 1) * L * m;  // [2][n][2][m] carries hi / lo
+        const int NLf = n;  // forward local pass: levels with a prefix
+        // slot: [n][3][m] prefix state (forward) / reverse state (VJP); VJP:
+        // then [n][3][m] unwind state, [n-1][G][m] the group's P_1..P_{n-1},
+        // [2][n][2][m] the carries pi^{c+1} and rho^c split into hi / lo
+        float* const st = slot;
+        float* const ust = slot + (int64_t)3 * n * m;
+        float* const gtp = ust + (int64_t)3 * n * m;
+        float* const cyt = gtp + (int64_t)(n - 1) * G * m;
+        (void)L;
         if (MODE == MODE_VJP) {
             const double* rcc = I.rho + (int64_t)c * nm;
+            const double* pnx = I.pi + (int64_t)(c + 1) * nm;
             for (int el = tid; el < (int)nm; el += NT) {
                 const int j = el / m, e2 = el % m;
-                const Carry<float> a = split_carry<float>(riem0 ? 0.0 : pic[el]);
+                const Carry<float> a = split_carry<float>(pnx[el]);
                 const Carry<float> r = split_carry<float>(rcc[el]);
                 cyt[((int64_t)j * 2) * m + e2] = a.hi;
                 cyt[((int64_t)j * 2 + 1) * m + e2] = a.lo;
@@ -269,6 +224,7 @@ __global__ void __launch_bounds__(NT, 2)
             }
         }
 
+        if (MODE == MODE_LOCAL) {
         // ---------------- forward state at the chunk start ----------------
         for (int j = 1; j <= NLf; ++j)
             for (int el = tid; el < m; el += NT) {
@@ -276,30 +232,6 @@ __global__ void __launch_bounds__(NT, 2)
                 st[(j - 1) * 3 * m + m + el] = 0.f;
                 st[(j - 1) * 3 * m + 2 * m + el] = (j == 1) ? __ldg(Ag + el) : 0.f;
             }
-        if (MODE == MODE_VJP && !riem0 && NLf >= 2) {
-            // f0_j = A[b] P_{j-1}[b] = A[b] pi_{j-1} for j = 2..NLf (FP32 FMA, once per chunk)
-            float* sA0 = sw;            // A[b], row pitch WP
-            float* sPi = sw + 32 * WP;  // pi_{j-1}
-            for (int el = tid; el < m; el += NT) sA0[(el >> 5) * WP + (el & 31)] = __ldg(Ag + el);
-            for (int j = 2; j <= NLf; ++j) {
-                __syncthreads();
-                for (int el = tid; el < m; el += NT)
-                    sPi[(el >> 5) * WP + (el & 31)] = (float)pic[(int64_t)(j - 2) * m + el];
-                __syncthreads();
-#pragma unroll
-                for (int q = 0; q < NP; ++q) {
-                    const int r = prow(q), cc = pcol(q);
-                    float s0 = 0.f, s1 = 0.f;
-                    for (int k = 0; k < D; ++k) {
-                        const float a = sA0[r * WP + k];
-                        const float2 pv = *reinterpret_cast<const float2*>(sPi + k * WP + cc);
-                        s0 = fmaf(a, pv.x, s0);
-                        s1 = fmaf(a, pv.y, s1);
-                    }
-                    *reinterpret_cast<float2*>(st + (j - 1) * 3 * m + 2 * m + r * D + cc) = make_float2(s0, s1);
-                }
-            }
-        }
         __syncthreads();
 
         // ---------------- forward over the groups ----------------
@@ -357,22 +289,36 @@ __global__ void __launch_bounds__(NT, 2)
                 // prefix pass of level j over the group's samples
                 {
                     float* sj = st + (j - 1) * 3 * m;
+                    // all of the group's inputs are loaded before any output
+                    // is stored, and full groups take a branch-free body, so
+                    // the element chains interleave
+                    auto pass = [&](auto fullc) {
+                        constexpr bool FULL = decltype(fullc)::value;
+                        float2 f[G][NP];
 #pragma unroll
-                    for (int l = 0; l < G; ++l) {
-                        if (l < ge) {
+                        for (int l = 0; l < G; ++l)
 #pragma unroll
-                            for (int q = 0; q < NP; ++q) {
-                                const int r = prow(q), cc = pcol(q);
-                                const float2 f = *reinterpret_cast<const float2*>(sw + (l * 32 + r) * WP + cc);
-                                const float P0 = fwd_step<float, RULE, MODE != MODE_LOCAL>(fs[q][0], f.x, 1 + l, kc, fcy[q][0]);
-                                const float P1 = fwd_step<float, RULE, MODE != MODE_LOCAL>(fs[q][1], f.y, 1 + l, kc, fcy[q][1]);
-                                if (j < NLf) put_pair(xb + l * 3 * PT, r, cc, P0, P1);
-                                if (MODE == MODE_VJP)
-                                    *reinterpret_cast<float2*>(tape + ((int64_t)(j - 1) * L + li0 + l) * m + r * D + cc) =
-                                        make_float2(P0, P1);
+                            for (int q = 0; q < NP; ++q)
+                                f[l][q] = (FULL || l < ge)
+                                              ? *reinterpret_cast<const float2*>(sw + (l * 32 + prow(q)) * WP + pcol(q))
+                                              : make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int l = 0; l < G; ++l) {
+                            if (FULL || l < ge) {
+#pragma unroll
+                                for (int q = 0; q < NP; ++q) {
+                                    const int r = prow(q), cc = pcol(q);
+                                    const float P0 =
+                                        fwd_step<float, RULE, false>(fs[q][0], f[l][q].x, 1 + l, kc, fcy[q][0]);
+                                    const float P1 =
+                                        fwd_step<float, RULE, false>(fs[q][1], f[l][q].y, 1 + l, kc, fcy[q][1]);
+                                    if (j < NLf) put_pair(xb + l * 3 * PT, r, cc, P0, P1);
+                                }
                             }
                         }
-                    }
+                    };
+                    if (ge == G) pass(std::true_type{});
+                    else pass(std::false_type{});
 #pragma unroll
                     for (int q = 0; q < NP; ++q) {
                         const int el = 2 * (tid + NT * q);
@@ -384,36 +330,78 @@ __global__ void __launch_bounds__(NT, 2)
                 __syncthreads();
                 if (j < NLf) {
                     load_fstate(j + 1);
-                    if (warp < ge) {
-                        float am[2][4][4], as[2][4][4];
+                    if (ws < ge) {
+                        float am[2][2][4], as[2][2][4];
                         zero_acc(am);
                         zero_acc(as);
-                        warp_product<false, false>(sxa + warp * 3 * PT, sxb + warp * 3 * PT, am, as, lane);
-                        store_acc(sw + warp * 32 * WP, am, as, g8, t4);
+                        warp_product<false, false>(sxa + ws * 3 * PT, sxb + ws * 3 * PT, am, as, lane, nh);
+                        store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh);
                     }
                     __syncthreads();
                 }
             }
         }
 
-        if (MODE == MODE_LOCAL && alive) {
+        if (alive) {
             for (int j = 1; j <= n; ++j)
                 for (int el = tid; el < m; el += NT)
                     I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] =
                         (double)st[(j - 1) * 3 * m + el] + (double)st[(j - 1) * 3 * m + m + el];
         }
+        }  // MODE_LOCAL
 
         if (MODE == MODE_VJP && alive) {
-            // the tape written above is read back by bulk copies (async proxy)
-            asm volatile("fence.proxy.async.global;" ::: "memory");
-            __syncthreads();
+            // ============ VJP: per group, backwards from the chunk end ============
+            // The prefix values P_j of the group's samples are rebuilt from the
+            // values at the group's end (at the chunk end: P_j[e] = pi^{c+1}_j)
+            // by running each block rule backwards (compensated), with
+            // W_j = A P_{j-1} recomputed on the tensor cores; they go through
+            // a small per-CTA buffer (L2) to the adjoint.  No replay of the
+            // chunk and no chunk-long tape through HBM.
+            const RuleCoef<float> kr = kc;
+            float* dAg = static_cast<float*>(I.dA) + b * m;
+            const float* Ae = Ag + (int64_t)Kp * m;  // the chunk end sample
+            auto ring = [](int li) { return li % 5; };
+            // reverse state zero, unwind state at the chunk end
             for (int j = 1; j <= n; ++j)
                 for (int el = tid; el < m; el += NT) {
-                    st[(j - 1) * 3 * m + el] = 0.f;          // Rb (local)
-                    st[(j - 1) * 3 * m + m + el] = 0.f;      // its compensation
-                    st[(j - 1) * 3 * m + 2 * m + el] = 0.f;  // pend
+                    st[(j - 1) * 3 * m + el] = 0.f;
+                    st[(j - 1) * 3 * m + m + el] = 0.f;
+                    st[(j - 1) * 3 * m + 2 * m + el] = 0.f;
                 }
-            float* dAg = static_cast<float*>(I.dA) + b * m;
+            for (int j = 1; j < n; ++j)
+                for (int el = tid; el < m; el += NT) {
+                    ust[(j - 1) * 3 * m + el] = cyt[((int64_t)(j - 1) * 2) * m + el];
+                    ust[(j - 1) * 3 * m + m + el] = cyt[((int64_t)(j - 1) * 2 + 1) * m + el];
+                    if (j == 1) ust[2 * m + el] = __ldg(Ae + el);
+                }
+            for (int i4 = tid; i4 < m / 4; i4 += NT)
+                put_quad(xa + ring(Kp) * 3 * PT, (i4 * 4) >> 5, (i4 * 4) & 31, __ldg(reinterpret_cast<const float4*>(Ae) + i4));
+            if (n > 2) {
+                // W_j[e] = A[e] pi^{c+1}_{j-1} for j = 2..n-1 (FP32 FMA, once per chunk)
+                float* sA0 = sw;
+                float* sPi = sw + 32 * WP;
+                for (int el = tid; el < m; el += NT) sA0[(el >> 5) * WP + (el & 31)] = __ldg(Ae + el);
+                for (int j = 2; j < n; ++j) {
+                    __syncthreads();
+                    for (int el = tid; el < m; el += NT)
+                        sPi[(el >> 5) * WP + (el & 31)] =
+                            cyt[((int64_t)(j - 2) * 2) * m + el] + cyt[((int64_t)(j - 2) * 2 + 1) * m + el];
+                    __syncthreads();
+#pragma unroll
+                    for (int q = 0; q < NP; ++q) {
+                        const int r = prow(q), cc = pcol(q);
+                        float s0 = 0.f, s1 = 0.f;
+                        for (int k = 0; k < D; ++k) {
+                            const float a = sA0[r * WP + k];
+                            const float2 pv = *reinterpret_cast<const float2*>(sPi + k * WP + cc);
+                            s0 = fmaf(a, pv.x, s0);
+                            s1 = fmaf(a, pv.y, s1);
+                        }
+                        *reinterpret_cast<float2*>(ust + (j - 1) * 3 * m + 2 * m + r * D + cc) = make_float2(s0, s1);
+                    }
+                }
+            }
             const int last0 = first + ((Kp - first) / G) * G;
             RevState<float> rs[NP][2];
             Carry<float> rcy[NP][2];
@@ -436,53 +424,168 @@ __global__ void __launch_bounds__(NT, 2)
                     }
                 }
             };
-            // staging uses, in order: A(group), P_{n-1}, ..., P_1 of the group, A(next group), ...
-            auto issue_tape = [&](int jt, int l0g) {
+            // bulk copies into sg, in order: a group's new samples (its anchor
+            // a = li0 - 1 through li0 + ge - 2; the group end is staged
+            // already), then P_{n-1}, ..., P_1 of the group, then the next
+            // group's new samples ...  sg offset s holds sample a + s.
+            auto issue_new = [&](int l0g) {
                 if (tid == 0) {
                     const int geg = min(G, Kp - l0g + 1);
+                    const int s0 = max(l0g - 1, 0);  // Riemann's first chunk has no anchor sample
+                    const int cnt = l0g + geg - 1 - s0;
                     tc::fence_async_smem();
-                    bulk_load(sg, tape + ((int64_t)(jt - 1) * L + l0g) * m, (uint32_t)geg * m * 4u, bar);
+                    bulk_load(sg + (s0 - (l0g - 1)) * m, Ag + (int64_t)s0 * m, (uint32_t)cnt * m * 4u, bar);
+                }
+            };
+            auto issue_tape = [&](int jt, int geg) {
+                if (tid == 0) {
+                    tc::fence_async_smem();
+                    bulk_load(sg, gtp + (int64_t)(jt - 1) * G * m, (uint32_t)geg * m * 4u, bar);
                 }
             };
             __syncthreads();
-            issue_group(last0);
+            issue_new(last0);
             for (int li0 = last0; li0 >= first && alive; li0 -= G) {
                 const int ge = min(G, Kp - li0 + 1);
+                const int a = li0 - 1;
+                const bool noa = riem0 && li0 == 0;
                 if (!wait_copy()) {
                     alive = false;
                     break;
                 }
                 for (int i4 = tid; i4 < ge * m / 4; i4 += NT) {
-                    const float4 v = reinterpret_cast<const float4*>(sg)[i4];
-                    const int s = (i4 * 4) / m, el = (i4 * 4) % m;
-                    put_quad(xa + s * 3 * PT, el >> 5, el & 31, v);
+                    const int so = (i4 * 4) / m, el = (i4 * 4) % m;
+                    if (!(noa && so == 0))
+                        put_quad(xa + ring(a + so) * 3 * PT, el >> 5, el & 31, reinterpret_cast<const float4*>(sg)[i4]);
                 }
                 __syncthreads();
-                if (n > 1) issue_tape(n - 1, li0);
-                else if (li0 - G >= first) issue_group(li0 - G);
+                // ---- unwind levels 1..n-1: P_j at the group's samples
+                for (int j = 1; j < n; ++j) {
+                    if (j > 1) {
+                        // W_j = A P_{j-1} at offsets 0..ge-1 (samples a .. a + ge - 1)
+                        if (ws < ge && !(noa && ws == 0)) {
+                            float am[2][2][4], as[2][2][4];
+                            zero_acc(am);
+                            zero_acc(as);
+                            warp_product<false, false>(sxa + ring(a + ws) * 3 * PT, sxb + ws * 3 * PT, am, as, lane, nh);
+                            store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh);
+                        }
+                        __syncthreads();
+                    }
+                    float* uj = ust + (j - 1) * 3 * m;
+                    float* gj = gtp + (int64_t)(j - 1) * G * m;
+                    auto pass = [&](auto fullc) {
+                        constexpr bool FULL = decltype(fullc)::value;
+                        const int gg = FULL ? G : ge;
+#pragma unroll
+                        for (int q = 0; q < NP; ++q) {
+                            const int r = prow(q), cc = pcol(q), el = 2 * (tid + NT * q);
+                            // W at offsets 0..G (G: the group end, carried)
+                            float W[2][G + 1];
+                            const float2 ph = *reinterpret_cast<const float2*>(uj + el);
+                            const float2 pl = *reinterpret_cast<const float2*>(uj + m + el);
+                            const float2 we = *reinterpret_cast<const float2*>(uj + 2 * m + el);
+#pragma unroll
+                            for (int so = 0; so < G; ++so) {
+                                float2 v = make_float2(0.f, 0.f);
+                                if (FULL || so < ge)
+                                    v = (j == 1) ? *reinterpret_cast<const float2*>(sg + so * m + el)
+                                                 : *reinterpret_cast<const float2*>(sw + (so * 32 + r) * WP + cc);
+                                W[0][so] = v.x;
+                                W[1][so] = v.y;
+                            }
+#pragma unroll
+                            for (int so = 0; so <= G; ++so)
+                                if (so == gg) {
+                                    W[0][so] = we.x;
+                                    W[1][so] = we.y;
+                                }
+                            float P[2][G];
+                            float hi[2] = {ph.x, ph.y}, lo[2] = {pl.x, pl.y};
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const float* w = W[h];
+                                if (RULE == R_BOOLE) {
+                                    // one block (a, a + 4]
+                                    const float inc = w[0] * kr.b14 + w[1] * kr.b64 + w[2] * kr.b24 + w[3] * kr.b64 + w[4] * kr.b14;
+                                    acc_add(hi[h], lo[h], -inc);
+                                    P[h][0] = hi[h] + lo[h];
+                                    P[h][1] = (w[1] * kr.h + w[0] * kr.h + lo[h]) + hi[h];
+                                    P[h][2] = (w[2] * kr.t3 + w[0] * kr.t3 + w[1] * kr.c4_3 + lo[h]) + hi[h];
+                                    P[h][3] = (w[3] * kr.c38 + w[0] * kr.c38 + w[1] * kr.c98 + w[2] * kr.c98 + lo[h]) + hi[h];
+                                } else if (RULE == R_SIMPSON) {
+                                    // blocks (a + 2, a + 4] (full groups) and (a, a + 2]
+                                    if (FULL || gg == 4) {
+                                        const float inc = w[4] * kr.t3 + w[2] * kr.t3 + w[3] * (4.f * kr.t3);
+                                        acc_add(hi[h], lo[h], -inc);
+                                        P[h][2] = hi[h] + lo[h];
+                                        P[h][3] = (w[3] * kr.h + w[2] * kr.h + lo[h]) + hi[h];
+                                    }
+                                    const float inc = w[2] * kr.t3 + w[0] * kr.t3 + w[1] * (4.f * kr.t3);
+                                    acc_add(hi[h], lo[h], -inc);
+                                    P[h][0] = hi[h] + lo[h];
+                                    P[h][1] = (w[1] * kr.h + w[0] * kr.h + lo[h]) + hi[h];
+                                } else {
+#pragma unroll
+                                    for (int so = G; so >= 1; --so) {
+                                        if (FULL || so <= gg) {
+                                            const float inc = (RULE == R_TRAP) ? w[so] * kr.h + w[so - 1] * kr.h : w[so] * kr.dt;
+                                            acc_add(hi[h], lo[h], -inc);
+                                            P[h][so - 1] = hi[h] + lo[h];
+                                        }
+                                    }
+                                }
+                            }
+                            // P_j at offsets 0..gg-1 as pieces (next level's
+                            // products), at the group's samples (offsets
+                            // 1..gg; gg: the previous group-end value) to the
+                            // group buffer, the new group-end state
+#pragma unroll
+                            for (int so = 0; so < G; ++so) {
+                                if ((FULL || so < ge) && j + 1 < n && !(noa && so == 0))
+                                    put_pair(xb + so * 3 * PT, r, cc, P[0][so], P[1][so]);
+                                if (so >= 1 && (FULL || so < ge))
+                                    *reinterpret_cast<float2*>(gj + (so - 1) * m + el) = make_float2(P[0][so], P[1][so]);
+                            }
+                            *reinterpret_cast<float2*>(gj + (gg - 1) * m + el) = make_float2(ph.x + pl.x, ph.y + pl.y);
+                            *reinterpret_cast<float2*>(uj + el) = make_float2(hi[0], hi[1]);
+                            *reinterpret_cast<float2*>(uj + m + el) = make_float2(lo[0], lo[1]);
+                            *reinterpret_cast<float2*>(uj + 2 * m + el) = make_float2(W[0][0], W[1][0]);
+                        }
+                    };
+                    if (ge == G) pass(std::true_type{});
+                    else pass(std::false_type{});
+                    __syncthreads();
+                }
+                // the group buffer was written by threads, is read by bulk copies
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                __syncthreads();
+                if (n > 1) issue_tape(n - 1, ge);
+                else if (li0 - G >= first) issue_new(li0 - G);
                 load_rstate(n);
                 // dA of the warp's sample: each level's product accumulates
                 // in fresh (main, small) accumulators, added here in FP32
-                float da[2][4][4];
+                float da[2][2][4];
                 zero_acc(da);
+                const uint32_t xas = sxa + ring(li0 + ws) * 3 * PT;
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
                         load_rstate(j);
-                        if (warp < ge) {
+                        if (ws < ge) {
                             // H_j = A^T G_{j+1} -> sw;  dA += G_{j+1} P_j^T
-                            float hm[2][4][4], hs[2][4][4];
+                            float hm[2][2][4], hs[2][2][4];
                             zero_acc(hm);
                             zero_acc(hs);
-                            warp_product<true, false>(sxa + warp * 3 * PT, sxb + warp * 3 * PT, hm, hs, lane);
-                            store_acc(sw + warp * 32 * WP, hm, hs, g8, t4);
-                            float tm[2][4][4], ts[2][4][4];
+                            warp_product<true, false>(xas, sxb + ws * 3 * PT, hm, hs, lane, nh);
+                            store_acc(sw + ws * 32 * WP, hm, hs, g8, t4, nh);
+                            float tm[2][2][4], ts[2][2][4];
                             zero_acc(tm);
                             zero_acc(ts);
-                            warp_product<false, true>(sxb + warp * 3 * PT, sxc + warp * 3 * PT, tm, ts, lane);
+                            warp_product<false, true>(sxb + ws * 3 * PT, sxc + ws * 3 * PT, tm, ts, lane, nh);
 #pragma unroll
                             for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                                for (int nt = 0; nt < 4; ++nt)
+                                for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
                                     for (int k = 0; k < 4; ++k) da[mt][nt][k] += tm[mt][nt][k] + ts[mt][nt][k];
                         }
@@ -492,21 +595,32 @@ __global__ void __launch_bounds__(NT, 2)
                     // FP32 into sw at level 1, for the final dA)
                     {
                         float* sj = st + (j - 1) * 3 * m;
+                        auto pass = [&](auto fullc) {
+                            constexpr bool FULL = decltype(fullc)::value;
+                            float2 h[G][NP];
 #pragma unroll
-                        for (int l = G - 1; l >= 0; --l) {
-                            if (l < ge) {
+                            for (int l = 0; l < G; ++l)
 #pragma unroll
-                                for (int q = 0; q < NP; ++q) {
-                                    const int r = prow(q), cc = pcol(q);
-                                    float2 h = make_float2(0.f, 0.f);
-                                    if (j < n) h = *reinterpret_cast<const float2*>(sw + (l * 32 + r) * WP + cc);
-                                    const float G0 = rev_step<float, RULE>(rs[q][0], h.x, 1 + l, kc, rcy[q][0]);
-                                    const float G1 = rev_step<float, RULE>(rs[q][1], h.y, 1 + l, kc, rcy[q][1]);
-                                    if (j > 1) put_pair(xb + l * 3 * PT, r, cc, G0, G1);
-                                    else *reinterpret_cast<float2*>(sw + (l * 32 + r) * WP + cc) = make_float2(G0, G1);
+                                for (int q = 0; q < NP; ++q)
+                                    h[l][q] = ((FULL || l < ge) && j < n)
+                                                  ? *reinterpret_cast<const float2*>(sw + (l * 32 + prow(q)) * WP + pcol(q))
+                                                  : make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int l = G - 1; l >= 0; --l) {
+                                if (FULL || l < ge) {
+#pragma unroll
+                                    for (int q = 0; q < NP; ++q) {
+                                        const int r = prow(q), cc = pcol(q);
+                                        const float G0 = rev_step<float, RULE>(rs[q][0], h[l][q].x, 1 + l, kc, rcy[q][0]);
+                                        const float G1 = rev_step<float, RULE>(rs[q][1], h[l][q].y, 1 + l, kc, rcy[q][1]);
+                                        if (j > 1) put_pair(xb + l * 3 * PT, r, cc, G0, G1);
+                                        else *reinterpret_cast<float2*>(sw + (l * 32 + r) * WP + cc) = make_float2(G0, G1);
+                                    }
                                 }
                             }
-                        }
+                        };
+                        if (ge == G) pass(std::true_type{});
+                        else pass(std::false_type{});
 #pragma unroll
                         for (int q = 0; q < NP; ++q) {
                             const int el = 2 * (tid + NT * q);
@@ -516,37 +630,37 @@ __global__ void __launch_bounds__(NT, 2)
                         }
                     }
                     if (j > 1) {
-                        // P_{j-1} from the tape (landed in sg) -> pieces in xc;
-                        // then the next copy: P_{j-2}, or A of the next group
+                        // P_{j-1} of the group (landed in sg) -> pieces in xc;
+                        // then the next copy: P_{j-2}, or the next group's samples
                         if (!wait_copy()) {
                             alive = false;
                             break;
                         }
                         for (int i4 = tid; i4 < ge * m / 4; i4 += NT) {
                             const float4 v = reinterpret_cast<const float4*>(sg)[i4];
-                            const int s = (i4 * 4) / m, el = (i4 * 4) % m;
-                            put_quad(xc + s * 3 * PT, el >> 5, el & 31, v);
+                            const int so = (i4 * 4) / m, el = (i4 * 4) % m;
+                            put_quad(xc + so * 3 * PT, el >> 5, el & 31, v);
                         }
                         __syncthreads();
-                        if (j > 2) issue_tape(j - 2, li0);
-                        else if (li0 - G >= first) issue_group(li0 - G);
+                        if (j > 2) issue_tape(j - 2, ge);
+                        else if (li0 - G >= first) issue_new(li0 - G);
                     } else {
                         __syncthreads();
                     }
                 }
                 if (!alive) break;
-                if (warp < ge) {
-                    const int li = li0 + warp;
+                if (ws < ge) {
+                    const int li = li0 + ws;
                     const bool shared = (li == Kp && c < I.C - 1);
                     float* row = dAg + (int64_t)li * m;
-                    const float* g1 = sw + warp * 32 * WP;
+                    const float* g1 = sw + ws * 32 * WP;
 #pragma unroll
                     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                        for (int nt = 0; nt < 4; ++nt)
+                        for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
                             for (int hh = 0; hh < 2; ++hh) {
-                                const int r = mt * 16 + g8 + 8 * hh, cc = nt * 8 + 2 * t4;
+                                const int r = mt * 16 + g8 + 8 * hh, cc = (2 * nh + nt) * 8 + 2 * t4;
                                 const float2 gv = *reinterpret_cast<const float2*>(g1 + r * WP + cc);
                                 const float v0 = da[mt][nt][2 * hh] + gv.x;
                                 const float v1 = da[mt][nt][2 * hh + 1] + gv.y;
