@@ -1053,8 +1053,7 @@ size_t mgb_plan_describe(const mgb_plan* plan, char* buf, size_t len) {
         // VJP on the warp-MMA kernel
         const char* kernel = !tc.use ? "k_chunk" : tc.family == 1 ? "k_small" : tc.family == 3 ? "k_bigtc"
                              : (tc.D == 32 && sg.variant == 2) ? "k_tiletc"
-                             : (tc.D == 32 && sg.variant == 3) ? "k_mma32"
-                             : (tc.D == 32 && sg.variant == 4) ? "k_mma32t" : "k_tile";
+                             : (tc.D == 32 && sg.variant == 3) ? "k_mma32" : "k_tile";
         const int ctas = !tc.use ? generic_ctas_per_sm(sg.variant % GENERIC_VARIANTS) : tc.ctas_per_sm;
         std::snprintf(tmp, sizeof(tmp),
                       "%s{\"d\": %d, \"instances\": %d, \"chunks\": %lld, \"kernel\": \"%s\", \"variant\": %d, "

@@ -1,6 +1,6 @@
 // Chunk kernel for the mixed form at d = 32 with every per-sample product on
-// the tensor cores through warp-level MMA (mma.sync m16n8k16, BF16 operands,
-// FP32 accumulators): the forward local pass and the VJP (replay + adjoint).
+// the tensor cores through warp-level MMA (mma.sync m16n8k16, FP16 operands,
+// FP32 accumulators): the forward local pass and the VJP.
 //
 // Why warp MMA at d = 32: the per-sample products W = A P, H = A^T G and
 // G P^T share no operand between samples, so a tcgen05 MMA (M >= 64) can only
@@ -10,30 +10,34 @@
 // 483 TFLOP/s of useful work for the block-diagonal tcgen05 batch and
 // 74 TFLOP/s on the FP32 FMA pipes.
 //
-// Precision: every FP32 operand is split exactly into three BF16 pieces
-// (x = x0 + x1 + x2) once, by the thread that produces it, and each product
-// is the sum of the six piece products with i + j <= 2.  X0 Y0 accumulates
-// alone and the five small terms together (the tensor core truncates each
-// accumulation step): measured 4.7e-8 relative per 32^3 product, against
-// 1.0e-7 for FP32 FMA (3.2e-7 with a single accumulator).
+// Precision: every FP32 operand matrix is scaled by a power of two from its
+// largest element and split exactly into two FP16 pieces once, by the
+// threads that produce it (mgb_mma.cuh); a product is the sum of three piece
+// products, X0 Y0 in its own accumulator and X0 Y1 + X1 Y0 in a second (the
+// tensor core truncates each accumulation step), rescaled in FP32.  The
+// scale needs the matrix's maximum before the split: each producing pass
+// reduces it per sample (warp max + one shared atomic per warp) and splits
+// after a barrier.
 //
 // Layout (one CTA of NW = 8 warps per chunk, samples in groups of G = 4 = a
 // Boole block; in the product phases warps 2s and 2s + 1 own sample s, each
 // one 32 x 16 column half of it, so that sixteen warps per SM (two CTAs)
 // hide the latency of the prefix and split work):
-//   xa  A as BF16 pieces, five sample slots        [5][3][32 x 32], swizzled
-//   xb  P_j (forward) or G_{j+1} (adjoint) pieces [G][3][32 x 32]
-//   xc  P_j of the group (adjoint)                 [G][3][32 x 32]
+//   xa  A as FP16 pieces, five sample slots        [5][2][32 x 32], swizzled
+//   xb  P_j (forward) or G_{j+1} (adjoint) pieces [G][2][32 x 32]
+//   xc  P_j of the group (adjoint), copied in as pieces from the group
+//       buffer                                     [G][2][32 x 32]
 //   sw  FP32 product outputs (prefix input)        [G][32][36]
-//   sg  FP32 staging of a bulk copy (A of a group's samples or one level of
-//       the group's P buffer)
+//   sg  FP32 staging of a bulk copy of A (a group's samples)
+//   mx / sk  per-sample maxima being reduced / scale exponents of the piece
+//       sets (A slots 0..4, xb 8..11; the group buffer's in the CTA's slot)
 // Piece tiles hold 64-byte rows with the 16-byte chunk c stored at c ^
 // ((row >> 1) & 3): ldmatrix of 8 rows and the prefix threads' row stores are
 // both free of bank conflicts.
 //
-// A of each group and (adjoint) each level of the group's P buffer arrive by
-// TMA bulk copies (cp.async.bulk, completion on an mbarrier), one copy ahead
-// of their use.  The adjoint needs every P_j at every sample in reverse
+// A of each group and (adjoint) each level of the group's P buffer (written
+// as scaled pieces by the backward rebuild) arrive by TMA bulk copies
+// (cp.async.bulk, completion on an mbarrier), one copy ahead of their use.  The adjoint needs every P_j at every sample in reverse
 // order; instead of replaying the chunk forward into a chunk-long tape (4 KB
 // per sample and level through HBM, twice), each group's P_j are rebuilt
 // backwards from the group end (the chunk end holds P_j = pi^{c+1}_j) by the
@@ -45,7 +49,6 @@
 // the SIMT kernel.  Every mbarrier wait is bounded; on time-out the CTA
 // waits (bounded) for its copy in flight, stops and raises the device flag.
 #include <cstdint>
-#include <cuda_bf16.h>
 #include <mutex>
 #include <type_traits>
 #include <vector>
@@ -64,19 +67,24 @@ constexpr int D = 32, m = D * D;
 constexpr int NW = 8, NT = 32 * NW, G = 4;
 constexpr int NP = m / 2 / NT;        // element pairs per thread per sample (2)
 constexpr int WP = 36;                // FP32 row pitch of sw
-constexpr uint32_t SX = G * 3 * PT;   // bytes per operand set
+constexpr uint32_t SET = NPC * PT;    // bytes of one sample's pieces
+constexpr uint32_t SX = G * SET;      // bytes per operand set
 // xa holds five sample sets: the VJP keeps A of a group's anchor and of its
 // four samples (a ring indexed by sample % 5)
-constexpr size_t OFF_XA = 0, OFF_XB = 5 * 3 * (size_t)PT, OFF_XC = OFF_XB + SX, OFF_W = OFF_XC + SX;
+constexpr size_t OFF_XA = 0, OFF_XB = 5 * (size_t)SET, OFF_XC = OFF_XB + SX, OFF_W = OFF_XC + SX;
 constexpr size_t OFF_SG = OFF_W + (size_t)G * 32 * WP * 4;
-constexpr size_t OFF_BAR = OFF_SG + (size_t)G * m * 4;
+constexpr size_t OFF_MX = OFF_SG + (size_t)G * m * 4;  // uint32 [2][8]
+constexpr size_t OFF_SK = OFF_MX + 64;                  // int [16]
+constexpr size_t OFF_BAR = OFF_SK + 64;
 constexpr size_t SMEM = OFF_BAR + 64;
+constexpr int SK_B = 8;  // scale-exponent slots of xb (A: 0..4)
 static_assert(NP * 2 * NT == m, "pair mapping");
+static_assert(m / 4 == NT, "one quad of every sample per thread");
 static_assert(SMEM + 1024 <= 114 * 1024, "two CTAs per SM");
 
 // One warp: acc (main, small) [mt][nt] += (X Y)[:, 16 nh .. 16 nh + 15] for
-// one sample, X and Y 32 x 32 given as BF16 piece tiles (3 tiles, PT bytes
-// apart) in row-major storage S:
+// one sample (scaled), X and Y 32 x 32 given as FP16 piece tiles (NPC tiles,
+// PT bytes apart) in row-major storage S:
 //   XT = false: X = S_x (rows m, cols k);  XT = true: X = S_x^T
 //   YT = false: Y = S_y (rows k, cols n);  YT = true: Y = S_y^T
 // The MMAs are issued piece pair by piece pair over the four output tiles,
@@ -88,14 +96,14 @@ __device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&a
     const int l8 = lane & 7, lb = (lane >> 3) & 1, lh = lane >> 4;
 #pragma unroll
     for (int ks = 0; ks < 2; ++ks) {
-        uint32_t bf[3][2][2];  // [piece][n-tile][reg]
-        uint32_t af[3][2][4];  // [piece][m-tile][reg]
+        uint32_t bf[NPC][2][2];  // [piece][n-tile][reg]
+        uint32_t af[NPC][2][4];  // [piece][m-tile][reg]
         {
             uint32_t o;
             if (!YT) o = toff(ks * 16 + l8 + 8 * lb, (2 * nh + lh) * 8);   // trans: rows k, cols n
             else o = toff((2 * nh + lh) * 8 + l8, ks * 16 + 8 * lb);        // rows n, cols k
 #pragma unroll
-            for (int p = 0; p < 3; ++p) {
+            for (int p = 0; p < NPC; ++p) {
                 uint32_t r[4];
                 if (!YT) ldsm4t(ys + p * PT + o, r);
                 else ldsm4(ys + p * PT + o, r);
@@ -111,21 +119,31 @@ __device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&a
             if (!XT) o = toff(mt * 16 + l8 + 8 * lb, ks * 16 + 8 * lh);   // rows m, cols k
             else o = toff(ks * 16 + l8 + 8 * lh, mt * 16 + 8 * lb);       // trans: rows k, cols m
 #pragma unroll
-            for (int p = 0; p < 3; ++p) {
+            for (int p = 0; p < NPC; ++p) {
                 if (!XT) ldsm4(xs + p * PT + o, af[p][mt]);
                 else ldsm4t(xs + p * PT + o, af[p][mt]);
             }
         }
-        // small terms (smallest first), then the main term
-        constexpr int PI[6] = {0, 2, 1, 0, 1, 0}, PJ[6] = {2, 0, 1, 1, 0, 0};
+        // the two small terms, then the main term
+        constexpr int PI[3] = {0, 1, 0}, PJ[3] = {1, 0, 0};
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
+        for (int q = 0; q < 3; ++q)
 #pragma unroll
             for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
                 for (int nt = 0; nt < 2; ++nt)
-                    mma16816(q == 5 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0], bf[PJ[q]][nt][1]);
+                    mma16816(q == 2 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0], bf[PJ[q]][nt][1]);
     }
+}
+
+// Factors undoing the operand scales 2^kx, 2^ky: v * u.a * u.b (two factors
+// keep each one a normal float)
+struct Unscale {
+    float a, b;
+};
+__device__ __forceinline__ Unscale unscale(int kx, int ky) {
+    const int k = kx + ky, k1 = min(126, max(-126, k));
+    return Unscale{pow2f(-k1), pow2f(k1 - k)};
 }
 
 __device__ __forceinline__ void zero_acc(float (&a)[2][2][4]) {
@@ -137,18 +155,19 @@ __device__ __forceinline__ void zero_acc(float (&a)[2][2][4]) {
             for (int k = 0; k < 4; ++k) a[i][j][k] = 0.f;
 }
 
-// FP32 output half-tile of one warp's product (main + small) into sw (pitch WP)
+// FP32 output half-tile of one warp's product (main + small, unscaled) into
+// sw (pitch WP)
 __device__ __forceinline__ void store_acc(float* o, const float (&am)[2][2][4], const float (&as)[2][2][4], int g8,
-                                          int t4, int nh) {
+                                          int t4, int nh, Unscale u) {
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 2; ++nt) {
             const int r = mt * 16 + g8, cc = (2 * nh + nt) * 8 + 2 * t4;
             *reinterpret_cast<float2*>(o + r * WP + cc) =
-                make_float2(am[mt][nt][0] + as[mt][nt][0], am[mt][nt][1] + as[mt][nt][1]);
+                make_float2((am[mt][nt][0] + as[mt][nt][0]) * u.a * u.b, (am[mt][nt][1] + as[mt][nt][1]) * u.a * u.b);
             *reinterpret_cast<float2*>(o + (r + 8) * WP + cc) =
-                make_float2(am[mt][nt][2] + as[mt][nt][2], am[mt][nt][3] + as[mt][nt][3]);
+                make_float2((am[mt][nt][2] + as[mt][nt][2]) * u.a * u.b, (am[mt][nt][3] + as[mt][nt][3]) * u.a * u.b);
         }
 }
 
@@ -163,6 +182,8 @@ __global__ void __launch_bounds__(NT, 2)
     float* const sw = reinterpret_cast<float*>(smem + OFF_W);
     float* const sg = reinterpret_cast<float*>(smem + OFF_SG);
     uint64_t* const bar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+    uint32_t* const mx = reinterpret_cast<uint32_t*>(smem + OFF_MX);
+    int* const sk = reinterpret_cast<int*>(smem + OFF_SK);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g8 = lane >> 2, t4 = lane & 3;
     const int ws = warp >> 1, nh = warp & 1;  // product phases: sample ws, column half nh
@@ -172,7 +193,20 @@ __global__ void __launch_bounds__(NT, 2)
         tc::mbar_init(bar);
         tc::mbar_init_fence();
     }
+    if (tid < 16) mx[tid] = 0u;
     __syncthreads();
+    // Scaled passes: every thread adds |value| bits of entry i (a sample of
+    // the pass) with mx_put (all lanes of every warp, uniformly), then after
+    // a barrier reads the entry's scale exponent with mx_get and splits; the
+    // pass ends with mx_done (the buffer of the following pass is cleared;
+    // a barrier always separates two scaled passes).
+    int par = 0;
+    auto mx_put = [&](int i, uint32_t u) { max_into(mx + par * 8 + i, u); };
+    auto mx_get = [&](int i) { return scale_exp(mx[par * 8 + i]); };
+    auto mx_done = [&]() {
+        if (tid < 8) mx[(par ^ 1) * 8 + tid] = 0u;
+        par ^= 1;
+    };
     uint32_t phase = 0;  // completed copies on bar
     bool alive = true;
     float* const slot = scratch + (int64_t)blockIdx.x * slot_elems;
@@ -187,6 +221,25 @@ __global__ void __launch_bounds__(NT, 2)
     // thread tid's element pairs: pair p = tid + NT q, elements 2p, 2p + 1
     auto prow = [&](int q) { return (tid + NT * q) >> 4; };
     auto pcol = [&](int q) { return ((tid + NT * q) & 15) * 2; };
+    // Scaled pass over up to G samples of FP32 data, quad tid of each
+    // (elements 4 tid .. 4 tid + 3): v[s] for s < cnt; sample s's pieces go
+    // to the set dst(s) (skipped when null), its exponent to sk[ski(s)].
+    auto stage_quads = [&](const float4 (&v)[G], int cnt, auto dst, auto ski) {
+#pragma unroll
+        for (int s2 = 0; s2 < G; ++s2) mx_put(s2, (s2 < cnt && dst(s2)) ? max4(v[s2]) : 0u);
+        __syncthreads();
+        const int r = (tid * 4) >> 5, cc = (tid * 4) & 31;
+#pragma unroll
+        for (int s2 = 0; s2 < G; ++s2) {
+            uint8_t* t = s2 < cnt ? dst(s2) : nullptr;
+            if (t) {
+                const int k = mx_get(s2);
+                put_quad(t, r, cc, v[s2], pow2f(k));
+                if (tid == 0) sk[ski(s2)] = k;
+            }
+        }
+        mx_done();
+    };
 
     for (int64_t w = blockIdx.x; w < nwork && alive; w += gridDim.x) {
         const ChunkRef wk = work[w];
@@ -203,12 +256,14 @@ __global__ void __launch_bounds__(NT, 2)
         const float* Ag = static_cast<const float*>(I.A) + b * m;
         const int NLf = n;  // forward local pass: levels with a prefix
         // slot: [n][3][m] prefix state (forward) / reverse state (VJP); VJP:
-        // then [n][3][m] unwind state, [n-1][G][m] the group's P_1..P_{n-1},
-        // [2][n][2][m] the carries pi^{c+1} and rho^c split into hi / lo
+        // then [n][3][m] unwind state, the group's P_1..P_{n-1} as scaled
+        // piece sets [n-1][G][SET bytes], [2][n][2][m] the carries pi^{c+1}
+        // and rho^c split into hi / lo, the piece sets' exponents [n-1][G]
         float* const st = slot;
         float* const ust = slot + (int64_t)3 * n * m;
-        float* const gtp = ust + (int64_t)3 * n * m;
-        float* const cyt = gtp + (int64_t)(n - 1) * G * m;
+        uint8_t* const gtp = reinterpret_cast<uint8_t*>(ust + (int64_t)3 * n * m);
+        float* const cyt = reinterpret_cast<float*>(gtp + (int64_t)(n - 1) * G * SET);
+        int* const gtk = reinterpret_cast<int*>(cyt + (int64_t)4 * n * m);
         (void)L;
         if (MODE == MODE_VJP) {
             const double* rcc = I.rho + (int64_t)c * nm;
@@ -276,11 +331,16 @@ __global__ void __launch_bounds__(NT, 2)
                 alive = false;
                 break;
             }
-            for (int i4 = tid; i4 < ge * m / 4; i4 += NT) {
-                const float4 v = reinterpret_cast<const float4*>(sg)[i4];
-                const int s = (i4 * 4) / m, el = (i4 * 4) % m, r = el >> 5, cc = el & 31;
-                *reinterpret_cast<float4*>(sw + (s * 32 + r) * WP + cc) = v;
-                put_quad(xa + s * 3 * PT, r, cc, v);
+            {
+                // A of the group: FP32 into sw (the level-1 prefix input),
+                // scaled pieces into xa
+                float4 v[G];
+#pragma unroll
+                for (int s2 = 0; s2 < G; ++s2) {
+                    v[s2] = s2 < ge ? reinterpret_cast<const float4*>(sg)[s2 * NT + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (s2 < ge) *reinterpret_cast<float4*>(sw + (s2 * 32 + ((tid * 4) >> 5)) * WP + ((tid * 4) & 31)) = v[s2];
+                }
+                stage_quads(v, ge, [&](int s2) { return xa + s2 * SET; }, [](int s2) { return s2; });
             }
             load_fstate(1);
             __syncthreads();
@@ -289,8 +349,9 @@ __global__ void __launch_bounds__(NT, 2)
                 // prefix pass of level j over the group's samples
                 {
                     float* sj = st + (j - 1) * 3 * m;
+                    float P[G][NP][2];
                     // all of the group's inputs are loaded before any output
-                    // is stored, and full groups take a branch-free body, so
+                    // is computed, and full groups take a branch-free body, so
                     // the element chains interleave
                     auto pass = [&](auto fullc) {
                         constexpr bool FULL = decltype(fullc)::value;
@@ -303,19 +364,16 @@ __global__ void __launch_bounds__(NT, 2)
                                               ? *reinterpret_cast<const float2*>(sw + (l * 32 + prow(q)) * WP + pcol(q))
                                               : make_float2(0.f, 0.f);
 #pragma unroll
-                        for (int l = 0; l < G; ++l) {
-                            if (FULL || l < ge) {
+                        for (int l = 0; l < G; ++l)
 #pragma unroll
-                                for (int q = 0; q < NP; ++q) {
-                                    const int r = prow(q), cc = pcol(q);
-                                    const float P0 =
-                                        fwd_step<float, RULE, false>(fs[q][0], f[l][q].x, 1 + l, kc, fcy[q][0]);
-                                    const float P1 =
-                                        fwd_step<float, RULE, false>(fs[q][1], f[l][q].y, 1 + l, kc, fcy[q][1]);
-                                    if (j < NLf) put_pair(xb + l * 3 * PT, r, cc, P0, P1);
+                            for (int q = 0; q < NP; ++q) {
+                                if (FULL || l < ge) {
+                                    P[l][q][0] = fwd_step<float, RULE, false>(fs[q][0], f[l][q].x, 1 + l, kc, fcy[q][0]);
+                                    P[l][q][1] = fwd_step<float, RULE, false>(fs[q][1], f[l][q].y, 1 + l, kc, fcy[q][1]);
+                                } else {
+                                    P[l][q][0] = P[l][q][1] = 0.f;
                                 }
                             }
-                        }
                     };
                     if (ge == G) pass(std::true_type{});
                     else pass(std::false_type{});
@@ -326,6 +384,29 @@ __global__ void __launch_bounds__(NT, 2)
                         *reinterpret_cast<float2*>(sj + m + el) = make_float2(fs[q][0].blo, fs[q][1].blo);
                         *reinterpret_cast<float2*>(sj + 2 * m + el) = make_float2(fs[q][0].f0, fs[q][1].f0);
                     }
+                    if (j < NLf) {
+                        // P_j of the group as scaled pieces (the next level's products)
+#pragma unroll
+                        for (int l = 0; l < G; ++l) {
+                            uint32_t u = 0u;
+#pragma unroll
+                            for (int q = 0; q < NP; ++q) u = max(u, max(absbits(P[l][q][0]), absbits(P[l][q][1])));
+                            mx_put(l, u);
+                        }
+                        __syncthreads();
+#pragma unroll
+                        for (int l = 0; l < G; ++l) {
+                            if (l < ge) {
+                                const int k = mx_get(l);
+                                const float sc = pow2f(k);
+#pragma unroll
+                                for (int q = 0; q < NP; ++q)
+                                    put_pair(xb + l * SET, prow(q), pcol(q), P[l][q][0], P[l][q][1], sc);
+                                if (tid == 0) sk[SK_B + l] = k;
+                            }
+                        }
+                        mx_done();
+                    }
                 }
                 __syncthreads();
                 if (j < NLf) {
@@ -334,8 +415,8 @@ __global__ void __launch_bounds__(NT, 2)
                         float am[2][2][4], as[2][2][4];
                         zero_acc(am);
                         zero_acc(as);
-                        warp_product<false, false>(sxa + ws * 3 * PT, sxb + ws * 3 * PT, am, as, lane, nh);
-                        store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh);
+                        warp_product<false, false>(sxa + ws * SET, sxb + ws * SET, am, as, lane, nh);
+                        store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh, unscale(sk[ws], sk[SK_B + ws]));
                     }
                     __syncthreads();
                 }
@@ -375,8 +456,14 @@ __global__ void __launch_bounds__(NT, 2)
                     ust[(j - 1) * 3 * m + m + el] = cyt[((int64_t)(j - 1) * 2 + 1) * m + el];
                     if (j == 1) ust[2 * m + el] = __ldg(Ae + el);
                 }
-            for (int i4 = tid; i4 < m / 4; i4 += NT)
-                put_quad(xa + ring(Kp) * 3 * PT, (i4 * 4) >> 5, (i4 * 4) & 31, __ldg(reinterpret_cast<const float4*>(Ae) + i4));
+            {
+                // A at the chunk end as scaled pieces
+                float4 v[G];
+                v[0] = __ldg(reinterpret_cast<const float4*>(Ae) + tid);
+#pragma unroll
+                for (int s2 = 1; s2 < G; ++s2) v[s2] = make_float4(0.f, 0.f, 0.f, 0.f);
+                stage_quads(v, 1, [&](int) { return xa + ring(Kp) * SET; }, [&](int) { return ring(Kp); });
+            }
             if (n > 2) {
                 // W_j[e] = A[e] pi^{c+1}_{j-1} for j = 2..n-1 (FP32 FMA, once per chunk)
                 float* sA0 = sw;
@@ -424,10 +511,11 @@ __global__ void __launch_bounds__(NT, 2)
                     }
                 }
             };
-            // bulk copies into sg, in order: a group's new samples (its anchor
-            // a = li0 - 1 through li0 + ge - 2; the group end is staged
-            // already), then P_{n-1}, ..., P_1 of the group, then the next
-            // group's new samples ...  sg offset s holds sample a + s.
+            // bulk copies, one in flight, in order: a group's new samples
+            // into sg (its anchor a = li0 - 1 through li0 + ge - 2, sg offset
+            // s holding sample a + s; the group end is staged already), then
+            // P_{n-1}, ..., P_1 of the group as pieces into xc, then the next
+            // group's new samples ...
             auto issue_new = [&](int l0g) {
                 if (tid == 0) {
                     const int geg = min(G, Kp - l0g + 1);
@@ -437,10 +525,11 @@ __global__ void __launch_bounds__(NT, 2)
                     bulk_load(sg + (s0 - (l0g - 1)) * m, Ag + (int64_t)s0 * m, (uint32_t)cnt * m * 4u, bar);
                 }
             };
+            // P_jt of the group, as pieces, straight into xc
             auto issue_tape = [&](int jt, int geg) {
                 if (tid == 0) {
                     tc::fence_async_smem();
-                    bulk_load(sg, gtp + (int64_t)(jt - 1) * G * m, (uint32_t)geg * m * 4u, bar);
+                    bulk_load(xc, gtp + (int64_t)(jt - 1) * G * SET, (uint32_t)geg * SET, bar);
                 }
             };
             __syncthreads();
@@ -453,10 +542,16 @@ __global__ void __launch_bounds__(NT, 2)
                     alive = false;
                     break;
                 }
-                for (int i4 = tid; i4 < ge * m / 4; i4 += NT) {
-                    const int so = (i4 * 4) / m, el = (i4 * 4) % m;
-                    if (!(noa && so == 0))
-                        put_quad(xa + ring(a + so) * 3 * PT, el >> 5, el & 31, reinterpret_cast<const float4*>(sg)[i4]);
+                {
+                    // A of the anchor and the new samples (sg offset so holds
+                    // sample a + so) as scaled pieces into the ring
+                    float4 v[G];
+#pragma unroll
+                    for (int s2 = 0; s2 < G; ++s2)
+                        v[s2] = s2 < ge ? reinterpret_cast<const float4*>(sg)[s2 * NT + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    stage_quads(
+                        v, ge, [&](int so) -> uint8_t* { return (noa && so == 0) ? nullptr : xa + ring(a + so) * SET; },
+                        [&](int so) { return ring(a + so); });
                 }
                 __syncthreads();
                 // ---- unwind levels 1..n-1: P_j at the group's samples
@@ -467,13 +562,14 @@ __global__ void __launch_bounds__(NT, 2)
                             float am[2][2][4], as[2][2][4];
                             zero_acc(am);
                             zero_acc(as);
-                            warp_product<false, false>(sxa + ring(a + ws) * 3 * PT, sxb + ws * 3 * PT, am, as, lane, nh);
-                            store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh);
+                            warp_product<false, false>(sxa + ring(a + ws) * SET, sxb + ws * SET, am, as, lane, nh);
+                            store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh, unscale(sk[ring(a + ws)], sk[SK_B + ws]));
                         }
                         __syncthreads();
                     }
                     float* uj = ust + (j - 1) * 3 * m;
-                    float* gj = gtp + (int64_t)(j - 1) * G * m;
+                    uint8_t* gj = gtp + (int64_t)(j - 1) * G * SET;
+                    float Pk[NP][2][G + 1];  // P_j at offsets 0..G (gg: the group end)
                     auto pass = [&](auto fullc) {
                         constexpr bool FULL = decltype(fullc)::value;
                         const int gg = FULL ? G : ge;
@@ -500,7 +596,7 @@ __global__ void __launch_bounds__(NT, 2)
                                     W[0][so] = we.x;
                                     W[1][so] = we.y;
                                 }
-                            float P[2][G];
+                            float P[2][G] = {};
                             float hi[2] = {ph.x, ph.y}, lo[2] = {pl.x, pl.y};
 #pragma unroll
                             for (int h = 0; h < 2; ++h) {
@@ -536,18 +632,13 @@ __global__ void __launch_bounds__(NT, 2)
                                     }
                                 }
                             }
-                            // P_j at offsets 0..gg-1 as pieces (next level's
-                            // products), at the group's samples (offsets
-                            // 1..gg; gg: the previous group-end value) to the
-                            // group buffer, the new group-end state
+                            // P_j at offsets 0..gg (gg: the previous group-end
+                            // value), the new group-end state
 #pragma unroll
-                            for (int so = 0; so < G; ++so) {
-                                if ((FULL || so < ge) && j + 1 < n && !(noa && so == 0))
-                                    put_pair(xb + so * 3 * PT, r, cc, P[0][so], P[1][so]);
-                                if (so >= 1 && (FULL || so < ge))
-                                    *reinterpret_cast<float2*>(gj + (so - 1) * m + el) = make_float2(P[0][so], P[1][so]);
+                            for (int so = 0; so <= G; ++so) {
+                                Pk[q][0][so] = so < gg ? P[0][so < G ? so : 0] : so == gg ? ph.x + pl.x : 0.f;
+                                Pk[q][1][so] = so < gg ? P[1][so < G ? so : 0] : so == gg ? ph.y + pl.y : 0.f;
                             }
-                            *reinterpret_cast<float2*>(gj + (gg - 1) * m + el) = make_float2(ph.x + pl.x, ph.y + pl.y);
                             *reinterpret_cast<float2*>(uj + el) = make_float2(hi[0], hi[1]);
                             *reinterpret_cast<float2*>(uj + m + el) = make_float2(lo[0], lo[1]);
                             *reinterpret_cast<float2*>(uj + 2 * m + el) = make_float2(W[0][0], W[1][0]);
@@ -555,6 +646,45 @@ __global__ void __launch_bounds__(NT, 2)
                     };
                     if (ge == G) pass(std::true_type{});
                     else pass(std::false_type{});
+                    {
+                        // P_j as scaled pieces: offsets 0..ge-1 into xb (the
+                        // next level's products), the group's samples (offsets
+                        // 1..gg) to the group buffer (the adjoint's G P^T),
+                        // one exponent per offset
+                        const int gg = ge;
+                        const bool nxt = j + 1 < n;
+#pragma unroll
+                        for (int so = 0; so <= G; ++so) {
+                            uint32_t u = 0u;
+                            if (so <= gg && !(noa && so == 0)) {
+#pragma unroll
+                                for (int q = 0; q < NP; ++q)
+                                    u = max(u, max(absbits(Pk[q][0][so]), absbits(Pk[q][1][so])));
+                            }
+                            mx_put(so, u);
+                        }
+                        __syncthreads();
+#pragma unroll
+                        for (int so = 0; so <= G; ++so) {
+                            if (so <= gg) {
+                                const int k = mx_get(so);
+                                const float sc = pow2f(k);
+                                if (nxt && so < gg && !(noa && so == 0)) {
+#pragma unroll
+                                    for (int q = 0; q < NP; ++q)
+                                        put_pair(xb + so * SET, prow(q), pcol(q), Pk[q][0][so], Pk[q][1][so], sc);
+                                    if (tid == 0) sk[SK_B + so] = k;
+                                }
+                                if (so >= 1) {
+#pragma unroll
+                                    for (int q = 0; q < NP; ++q)
+                                        put_pair(gj + (so - 1) * SET, prow(q), pcol(q), Pk[q][0][so], Pk[q][1][so], sc);
+                                    if (tid == 0) gtk[(j - 1) * G + so - 1] = k;
+                                }
+                            }
+                        }
+                        mx_done();
+                    }
                     __syncthreads();
                 }
                 // the group buffer was written by threads, is read by bulk copies
@@ -567,34 +697,40 @@ __global__ void __launch_bounds__(NT, 2)
                 // in fresh (main, small) accumulators, added here in FP32
                 float da[2][2][4];
                 zero_acc(da);
-                const uint32_t xas = sxa + ring(li0 + ws) * 3 * PT;
+                const uint32_t xas = sxa + ring(li0 + ws) * SET;
                 for (int j = n; j >= 1; --j) {
                     if (j < n) {
                         load_rstate(j);
                         if (ws < ge) {
                             // H_j = A^T G_{j+1} -> sw;  dA += G_{j+1} P_j^T
+                            const int kp = gtk[(j - 1) * G + ws];
                             float hm[2][2][4], hs[2][2][4];
                             zero_acc(hm);
                             zero_acc(hs);
-                            warp_product<true, false>(xas, sxb + ws * 3 * PT, hm, hs, lane, nh);
-                            store_acc(sw + ws * 32 * WP, hm, hs, g8, t4, nh);
+                            warp_product<true, false>(xas, sxb + ws * SET, hm, hs, lane, nh);
+                            store_acc(sw + ws * 32 * WP, hm, hs, g8, t4, nh, unscale(sk[ring(li0 + ws)], sk[SK_B + ws]));
                             float tm[2][2][4], ts[2][2][4];
                             zero_acc(tm);
                             zero_acc(ts);
-                            warp_product<false, true>(sxb + ws * 3 * PT, sxc + ws * 3 * PT, tm, ts, lane, nh);
+                            warp_product<false, true>(sxb + ws * SET, sxc + ws * SET, tm, ts, lane, nh);
+                            const Unscale u = unscale(sk[SK_B + ws], kp);
 #pragma unroll
                             for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
                                 for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
-                                    for (int k = 0; k < 4; ++k) da[mt][nt][k] += tm[mt][nt][k] + ts[mt][nt][k];
+                                    for (int k = 0; k < 4; ++k) da[mt][nt][k] += (tm[mt][nt][k] + ts[mt][nt][k]) * u.a * u.b;
                         }
                     }
                     __syncthreads();
-                    // reverse prefix pass of level j: G_j -> pieces in xb (and
-                    // FP32 into sw at level 1, for the final dA)
+                    // the products above were the last readers of xc: P_{j-1}
+                    // of the group lands there during the reverse pass
+                    if (j < n && j > 1) issue_tape(j - 1, ge);
+                    // reverse prefix pass of level j: G_j -> scaled pieces in
+                    // xb (and FP32 into sw at level 1, for the final dA)
                     {
                         float* sj = st + (j - 1) * 3 * m;
+                        float Gv[G][NP][2];
                         auto pass = [&](auto fullc) {
                             constexpr bool FULL = decltype(fullc)::value;
                             float2 h[G][NP];
@@ -606,18 +742,16 @@ __global__ void __launch_bounds__(NT, 2)
                                                   ? *reinterpret_cast<const float2*>(sw + (l * 32 + prow(q)) * WP + pcol(q))
                                                   : make_float2(0.f, 0.f);
 #pragma unroll
-                            for (int l = G - 1; l >= 0; --l) {
-                                if (FULL || l < ge) {
+                            for (int l = G - 1; l >= 0; --l)
 #pragma unroll
-                                    for (int q = 0; q < NP; ++q) {
-                                        const int r = prow(q), cc = pcol(q);
-                                        const float G0 = rev_step<float, RULE>(rs[q][0], h[l][q].x, 1 + l, kc, rcy[q][0]);
-                                        const float G1 = rev_step<float, RULE>(rs[q][1], h[l][q].y, 1 + l, kc, rcy[q][1]);
-                                        if (j > 1) put_pair(xb + l * 3 * PT, r, cc, G0, G1);
-                                        else *reinterpret_cast<float2*>(sw + (l * 32 + r) * WP + cc) = make_float2(G0, G1);
+                                for (int q = 0; q < NP; ++q) {
+                                    if (FULL || l < ge) {
+                                        Gv[l][q][0] = rev_step<float, RULE>(rs[q][0], h[l][q].x, 1 + l, kc, rcy[q][0]);
+                                        Gv[l][q][1] = rev_step<float, RULE>(rs[q][1], h[l][q].y, 1 + l, kc, rcy[q][1]);
+                                    } else {
+                                        Gv[l][q][0] = Gv[l][q][1] = 0.f;
                                     }
                                 }
-                            }
                         };
                         if (ge == G) pass(std::true_type{});
                         else pass(std::false_type{});
@@ -628,22 +762,46 @@ __global__ void __launch_bounds__(NT, 2)
                             *reinterpret_cast<float2*>(sj + m + el) = make_float2(rs[q][0].rlo, rs[q][1].rlo);
                             *reinterpret_cast<float2*>(sj + 2 * m + el) = make_float2(rs[q][0].pend, rs[q][1].pend);
                         }
+                        if (j > 1) {
+#pragma unroll
+                            for (int l = 0; l < G; ++l) {
+                                uint32_t u = 0u;
+#pragma unroll
+                                for (int q = 0; q < NP; ++q) u = max(u, max(absbits(Gv[l][q][0]), absbits(Gv[l][q][1])));
+                                mx_put(l, u);
+                            }
+                            __syncthreads();
+#pragma unroll
+                            for (int l = 0; l < G; ++l) {
+                                if (l < ge) {
+                                    const int k = mx_get(l);
+                                    const float sc = pow2f(k);
+#pragma unroll
+                                    for (int q = 0; q < NP; ++q)
+                                        put_pair(xb + l * SET, prow(q), pcol(q), Gv[l][q][0], Gv[l][q][1], sc);
+                                    if (tid == 0) sk[SK_B + l] = k;
+                                }
+                            }
+                            mx_done();
+                        } else {
+#pragma unroll
+                            for (int l = 0; l < G; ++l)
+                                if (l < ge) {
+#pragma unroll
+                                    for (int q = 0; q < NP; ++q)
+                                        *reinterpret_cast<float2*>(sw + (l * 32 + prow(q)) * WP + pcol(q)) =
+                                            make_float2(Gv[l][q][0], Gv[l][q][1]);
+                                }
+                        }
                     }
                     if (j > 1) {
-                        // P_{j-1} of the group (landed in sg) -> pieces in xc;
-                        // then the next copy: P_{j-2}, or the next group's samples
+                        // P_{j-1} of the group has landed in xc; after P_1 the
+                        // next group's samples follow
                         if (!wait_copy()) {
                             alive = false;
                             break;
                         }
-                        for (int i4 = tid; i4 < ge * m / 4; i4 += NT) {
-                            const float4 v = reinterpret_cast<const float4*>(sg)[i4];
-                            const int so = (i4 * 4) / m, el = (i4 * 4) % m;
-                            put_quad(xc + so * 3 * PT, el >> 5, el & 31, v);
-                        }
-                        __syncthreads();
-                        if (j > 2) issue_tape(j - 2, ge);
-                        else if (li0 - G >= first) issue_new(li0 - G);
+                        if (j == 2 && li0 - G >= first) issue_new(li0 - G);
                     } else {
                         __syncthreads();
                     }

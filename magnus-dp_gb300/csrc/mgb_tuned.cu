@@ -489,12 +489,10 @@ cudaError_t launch_tile_m(int rule, int mode, const LaunchArgs& a, int grid, boo
 
 // variant 0: two CTAs per SM (if shared memory allows), 1: one; at d = 32
 // variant 2: the tcgen05 forward local pass with the warp-MMA VJP, 3: the
-// warp-MMA kernel (mgb_mma32.cu) for both, 4: its warp-tile form
-// (mgb_mma32t.cu) for both
+// warp-MMA kernel (mgb_mma32.cu) for both
 cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only) {
     if (D == 32 && variant >= 2) {
         if (variant == 2 && mode == MODE_LOCAL) return launch_tiletc(rule, a, grid, prepare_only);
-        if (variant == 4) return launch_mma32t(rule, mode, a, grid, prepare_only);
         return launch_mma32(rule, mode, a, grid, prepare_only);
     }
     if (variant >= 2) variant = 0;
@@ -548,7 +546,7 @@ TunedChoice choose_tuned(bool plain, int kind, int rule, int mode, bool f64io, c
     tc.family = 2;
     tc.D = D;
     tc.nmax = nmax;
-    tc.nvariants = smem <= 113 * 1024 ? (D == 32 ? 5 : 2) : 1;
+    tc.nvariants = smem <= 113 * 1024 ? (D == 32 ? 4 : 2) : 1;
     tc.variant = variant < tc.nvariants ? variant : 0;
     if (tc.nvariants == 1) tc.variant = 1;  // one CTA per SM only
     tc.ctas_per_sm = tc.variant == 1 ? 1 : 2;
@@ -573,7 +571,8 @@ SegSizing size_segment(bool plain, int kind, int rule, bool f64io, const std::ve
         Lmax = std::max(Lmax, L);
         generic = std::max<int64_t>(generic, (int64_t)(I.n + 4) * L * I.m + 7 * (int64_t)I.n * I.m);
         // the warp-MMA VJP at d = 32: reverse and unwind states, the group
-        // buffer of P_1..P_{n-1} and the split carries, (14 n - 4) m
+        // buffer of P_1..P_{n-1} (pieces), the split carries and the group
+        // buffer's exponents, (14 n - 4) m floats + 4 (n - 1) ints
         generic = std::max<int64_t>(generic, 14 * (int64_t)I.n * I.m);
     }
     // slots for the most resident CTAs any variant of the segment's kernel has

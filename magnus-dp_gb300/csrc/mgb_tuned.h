@@ -40,16 +40,12 @@ int big_variants(int D);
 int big_ctas_per_sm(int D, int variant);
 // Group-tiled kernel (mgb_tuned.cu), variant 0: 2 CTAs per SM, 1: one;
 // at d = 32 variant 2: the tcgen05 forward local pass (mgb_tiletc.cu) with
-// the warp-MMA VJP, variant 3: the warp-MMA kernel for both, variant 4: its
-// warp-tile form for both.
+// the warp-MMA VJP, variant 3: the warp-MMA kernel for both.
 cudaError_t launch_tile(int D, int rule, int mode, const LaunchArgs& a, int grid, int variant, bool prepare_only);
 cudaError_t launch_tiletc(int rule, const LaunchArgs& a, int grid, bool prepare_only);
 // Warp-MMA kernel at d = 32 (mgb_mma32.cu), forward local pass and VJP; two
 // CTAs per SM.
 cudaError_t launch_mma32(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only);
-// Its warp-tile form (mgb_mma32t.cu): each warp a 16 x 16 tile of every
-// sample of a group, prefix passes on the accumulators in registers.
-cudaError_t launch_mma32t(int rule, int mode, const LaunchArgs& a, int grid, bool prepare_only);
 // Device address of the time-out flag the tensor-core kernels raise.
 int* device_timeout_ptr();
 // One CTA waits (limit_ns) on an mbarrier nothing arrives at and raises the

@@ -57,8 +57,8 @@ RULES = {0: "Boole", 1: "Simpson", 2: "Trapezoid", 3: "Riemann"}
 
 
 @pytest.mark.parametrize("d,nvariants,precision,dtype_name,tol,kernel", [
-    # 2: tcgen05 forward + warp-MMA VJP, 3: warp-MMA forward and VJP, 4: warp-tile form
-    (32, 5, _lib.PRECISION_MIXED, "float32", 1e-6, ["k_tile", "k_tile", "k_tiletc", "k_mma32", "k_mma32t"]),
+    # 2: tcgen05 forward + warp-MMA VJP, 3: warp-MMA forward and VJP
+    (32, 4, _lib.PRECISION_MIXED, "float32", 1e-6, ["k_tile", "k_tile", "k_tiletc", "k_mma32"]),
     (16, 2, _lib.PRECISION_MIXED, "float32", 1e-6, "k_tile"),
     (64, 5, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),  # 4: one accumulator pair, 3 CTAs/SM
     (128, 3, _lib.PRECISION_MIXED, "float32", 1e-6, "k_bigtc"),  # 2: one accumulator pair, 2 CTAs/SM
@@ -88,8 +88,8 @@ def test_plan_reports_tuned_variant(cuda, monkeypatch):
     specs = [(32, 1025, 5)] * 4 + [(64, 513, 4)] * 2
     host, outs, dAs, desc = _run_plan(cuda, specs, _lib.PRECISION_MIXED, "float32", K=64)
     by_d = {s["d"]: s for s in desc["segments"]}
-    assert by_d[32]["kernel"] in ("k_tile", "k_tiletc", "k_mma32", "k_mma32t") and by_d[64]["kernel"] == "k_bigtc"
-    for seg, nv in ((by_d[32], 5), (by_d[64], 5)):
+    assert by_d[32]["kernel"] in ("k_tile", "k_tiletc", "k_mma32") and by_d[64]["kernel"] == "k_bigtc"
+    for seg, nv in ((by_d[32], 4), (by_d[64], 5)):
         ms = seg["tuned_ms"]
         assert len(ms) == nv and all(t > 0 for t in ms), seg
         assert ms[seg["variant"]] == min(ms), seg  # the fastest (ties: either)
