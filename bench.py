@@ -196,9 +196,37 @@ def oracle_check(A, cot, out, dA, n, t0, tf):
             "seconds": time.perf_counter() - t}
 
 
+def pinned_host(shape, np_dtype):
+    """Page-locked host tensor of exactly its size, from cudaHostAlloc through
+    the engine library's CUDA runtime (torch's pinned allocator, the same
+    kind of memory, rounds a block up to a power of two: 128 GB for the
+    68.7 GB of config4's A; numpy memory registered with cudaHostRegister
+    copied at 19-43 GB/s on the GB300 host against 66-211 GB/s).  Returns
+    (tensor, release)."""
+    import torch
+    rt = None
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            rt = ctypes.CDLL(name)
+            break
+        except OSError:
+            continue
+    if rt is None:
+        raise RuntimeError("CUDA runtime library not found")
+    count = int(np.prod(shape))
+    nbytes = count * np.dtype(np_dtype).itemsize
+    ptr = ctypes.c_void_p()
+    rc = rt.cudaHostAlloc(ctypes.byref(ptr), ctypes.c_size_t(nbytes), ctypes.c_uint(0))
+    if rc != 0:
+        raise RuntimeError(f"cudaHostAlloc of {nbytes} bytes failed with CUDA error {rc}")
+    buf = (ctypes.c_char * nbytes).from_address(ptr.value)
+    arr = np.frombuffer(buf, dtype=np_dtype, count=count).reshape(shape)
+    return torch.from_numpy(arr), (lambda: rt.cudaFreeHost(ptr))
+
+
 def e2e_instances(B, bytes_per_instance):
     """Instances for the end-to-end legs: the whole batch when page-locked
-    host buffers for its input and dA (two copies) fit in half of the host's
+    host buffers for its input and dA (two copies) fit in 70 % of the host's
     available memory, else as many as do."""
     avail = None
     try:
@@ -210,7 +238,7 @@ def e2e_instances(B, bytes_per_instance):
         pass
     if avail is None:
         return min(B, 128)
-    return max(1, min(B, int(0.5 * avail // (2 * bytes_per_instance))))
+    return max(1, min(B, int(0.7 * avail // (2 * bytes_per_instance))))
 
 
 def cpu_model():
@@ -307,15 +335,17 @@ def kernel_roofs(kernels, steps, B, S, d, n, K, plain=False):
     from the library's launch timing), per launch:
 
       chunk_local  (n-1) products of 2 d^3 flop per sample; reads A once
-      chunk_vjp    3 (n-1) products per sample (replay, A^T G, G P^T); reads
-                   A twice, writes dA
+      chunk_vjp    3 (n-1) products per sample (forward recomputation,
+                   A^T G, G P^T); reads A once, writes dA
       scan, rscan  n(n-1)/2 d x d products per chunk step; read the chunk
                    transfers, write the chunk states (FP64 arrays)
       fin_*        the per-instance FP64 algebra (latency-bound, no roof)
 
-    Mixed-form products on the tensor cores are FP32-accurate emulations from
-    BF16 pieces, so their roof is the measured sustained BF16 rate / 3 (the
-    three-product BF16x3 convention).  The mixed-form scans run double-FP32
+    Mixed-form products on the tensor cores are FP32-accurate emulations:
+    three MMAs per product on two scaled FP16 pieces per operand (d = 32) or
+    six on three BF16 pieces (d = 64/128), so their roof is the measured
+    sustained BF16 rate / 3 (FP16 and BF16 dense rates are equal on this
+    part).  The mixed-form scans run double-FP32
     arithmetic on the FP32 pipes (about six FP32 flops per emulated flop):
     roof = nominal FP32 rate (152 SMs x 128 lanes x 2 x max clock) / 6.  The
     plain form's products and scans are rated against the nominal FP64 rate
@@ -330,16 +360,16 @@ def kernel_roofs(kernels, steps, B, S, d, n, K, plain=False):
         prod_roof = (fp64_nominal, "fp64", "nominal FP64")
         scan_roof = prod_roof
     else:
-        prod_roof = (bf16_sustained_peak() / 3, "tensor", "BF16x3 = measured sustained BF16 / 3")
+        prod_roof = (bf16_sustained_peak() / 3, "tensor", "3 MMAs per product = measured sustained BF16 / 3")
         scan_roof = (fp32_nominal / 6, "fp32", "double-FP32 = nominal FP32 / 6")
     work = {
         "chunk_local": ((n - 1) * 2.0 * d ** 3 * S * B, S * m * 4.0 * B, prod_roof),
-        "chunk_vjp": (3 * (n - 1) * 2.0 * d ** 3 * S * B, 3 * S * m * 4.0 * B, prod_roof),
+        "chunk_vjp": (3 * (n - 1) * 2.0 * d ** 3 * S * B, 2 * S * m * 4.0 * B, prod_roof),
         "scan": (n * (n - 1) / 2 * 2.0 * d ** 3 * C * B, (2 * C + 1) * n * m * 8.0 * B, scan_roof),
         "rscan": (n * (n - 1) / 2 * 2.0 * d ** 3 * C * B, (2 * C) * n * m * 8.0 * B, scan_roof),
     }
     out = {}
-    for name, (launches, total_ms) in kernels.items():
+    for name, (launches, total_ms, *_) in kernels.items():
         launch_ms = total_ms / max(launches, 1)
         per = launches / steps  # launches per step
         flops, nbytes, (fpeak, fbound, fsrc) = work.get(name, (0.0, 0.0, (None, None, None)))
@@ -804,10 +834,10 @@ def main():
 
         # ---- end to end through the public autograd API, pinned host buffers
         eb = min(args.e2e_batch, B) if args.e2e_batch > 0 else e2e_instances(B, S * d * d * 4)
-        A_host = torch.empty((eb, S, d, d), dtype=torch.float32, pin_memory=True)
+        A_host, free_A_host = pinned_host((eb, S, d, d), np.float32)
         A_host.copy_(A[:eb])
         cot_host = cot[:eb].cpu().pin_memory()
-        dA_host = torch.empty_like(A_host).pin_memory()
+        dA_host, free_dA_host = pinned_host((eb, S, d, d), np.float32)
         out_host = torch.empty((eb, d, d), dtype=torch.float32).pin_memory()
         del graph
         _lib.check(lib.mgb_plan_destroy(plan))
@@ -878,16 +908,28 @@ def main():
         prof_wall = (time.perf_counter() - t0h) * 1e3
         lib.mgb_profile_enable(0)
         stages = _lib.profile_read(reset=True)
-        stage_ms = {"h2d": stages.get("h2d", (0, 0.0))[1], "d2h": stages.get("d2h", (0, 0.0))[1],
-                    "kernels": sum(v[1] for k, v in stages.items() if k not in ("h2d", "d2h")), "wall": prof_wall}
+        def stage_sum(prefix):
+            return sum(v[1] for k, v in stages.items() if k.startswith(prefix + "."))
+
+        stage_ms = {"h2d": stage_sum("h2d"), "d2h": stage_sum("d2h"),
+                    "kernels": sum(v[1] for k, v in stages.items() if "." not in k), "wall": prof_wall}
+        # per sub-batch: [start, end] of its copies in, kernels and copies out
+        # (ms after the first copy started)
+        subs = sorted(int(k.split(".")[1]) for k in stages if k.startswith("comp."))
+        t_first = min((v[2] for k, v in stages.items() if "." in k), default=0.0)
+        timeline = [{st: [round(stages[f"{st}.{b}"][2] - t_first, 2), round(stages[f"{st}.{b}"][3] - t_first, 2)]
+                     for st in ("h2d", "comp", "d2h") if f"{st}.{b}" in stages} for b in subs]
         result["e2e"] = {"value": eb * S * n / (host_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h, "instances": eb, "ms_per_step": host_ms,
                          "ms_per_step_min_max": [min(host_ms_all), max(host_ms_all)], "steps": len(host_ms_all),
                          "api": "mgb_fwd_vjp_host_batched (C ABI, host buffers, synchronous; wall clock, median "
                                 "of 5 calls: host-to-device copy rates on this machine vary between calls)",
-                         "stage_ms_one_call": stage_ms,
+                         "stage_ms_one_call": stage_ms, "sub_batches_ms": timeline,
                          "link_gbs": {"h2d": h2d / (stage_ms["h2d"] / 1e3) / 1e9 if stage_ms["h2d"] else None,
                                       "d2h": d2h / (stage_ms["d2h"] / 1e3) / 1e9 if stage_ms["d2h"] else None}}
+        del A_host, dA_host
+        free_A_host()
+        free_dA_host()
 
         # ---- CPU baseline (oracle port on the host cores, bounded sample)
         threads = os.cpu_count() or 1

@@ -142,13 +142,14 @@ mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, vo
 /* Engine-specific (the reference makes one compute(record_vjp=True) and one
  * compute_vjp(vjp_data) call per instance, src/api/pybind.cpp:357-433): the
  * forward (out) and the VJP (dA) of `count` instances from HOST buffers in
- * one synchronous call.  Instances go to the device in sub-batches
- * (MGB_HOST_SUBBATCHES, default 4, of at least 256 MB each) through three
- * rotating device slots, so the host-to-device copy of one sub-batch, the
- * kernels of the previous one and the device-to-host copy of the one before
- * overlap.  Host buffers should be page-locked (cudaMallocHost /
- * cudaHostRegister / torch pin_memory) for the copies to overlap; pageable
- * ones are correct but staged by the driver.  The slots stay allocated on
+ * one synchronous call.  Instances go to the device in sub-batches of at
+ * least 256 MB (by default ramped: 1, 3, 4, 4, 3, 1 sixteenths of the input;
+ * MGB_HOST_SUBBATCHES = p cuts p equal ones) through three rotating device
+ * slots, so the host-to-device copy of one sub-batch, the kernels of the
+ * previous one and the device-to-host copy of the one before overlap.  Host
+ * buffers should be page-locked (cudaHostAlloc / cudaMallocHost / torch
+ * pin_memory) for the copies to overlap; pageable ones are correct but
+ * staged by the driver.  The slots stay allocated on
  * the device for later calls (calls are serialized inside the library). */
 mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, const void* const* A,
                                     const void* const* cot, void* const* out, void* const* dA);
@@ -197,15 +198,20 @@ mgb_status mgb_device_check(void);
 mgb_status mgb_selftest_bounded_wait(int64_t limit_ns, void* stream);
 
 /* Kernel timing.  While enabled, every engine kernel launch is bracketed by
- * CUDA events on its stream; mgb_profile_read waits for the recorded events,
- * fills up to `capacity` entries (one per kernel name: launches and total
- * milliseconds) and returns the number of names.  For benchmarking only: the
- * events add a few microseconds per launch.  No reference counterpart (the
- * reference has no tracing). */
+ * CUDA events on its stream, and mgb_fwd_vjp_host_batched brackets each
+ * sub-batch's stages ("h2d.<b>", "comp.<b>", "d2h.<b>"); mgb_profile_read
+ * waits for the recorded events, fills up to `capacity` entries (one per
+ * name: launches, total milliseconds, and the first start / last end in
+ * milliseconds after the moment timing was switched on) and returns the
+ * number of names.  For benchmarking only: the events add a few
+ * microseconds per launch.  No reference counterpart (the reference has no
+ * tracing). */
 typedef struct mgb_kernel_time {
     char name[40];
     uint64_t launches;
     double total_ms;
+    double first_start_ms;
+    double last_end_ms;
 } mgb_kernel_time;
 mgb_status mgb_profile_enable(int enable);
 size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset);

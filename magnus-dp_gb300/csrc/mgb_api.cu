@@ -60,9 +60,11 @@ struct ProfEvent {
 struct ProfTotal {
     uint64_t launches = 0;
     double ms = 0.0;
+    double first = 1e300, last = -1e300;  // ms from the reference event
 };
 std::mutex g_prof_mutex;
 bool g_prof_enabled = false;
+cudaEvent_t g_prof_ref = nullptr;  // recorded when timing is switched on
 std::vector<ProfEvent> g_prof_pending;
 std::vector<std::pair<std::string, ProfTotal>> g_prof_totals;
 
@@ -1272,15 +1274,32 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
         bck[i] = mgb_checkpoint_bytes(&probs[i]);
         total += bin[i];
     }
-    const int parts = std::max(1, env_int("MGB_HOST_SUBBATCHES", 4));
-    const size_t target = std::max<size_t>(total / (size_t)parts, (size_t)256 << 20);
+    // Sub-batches: MGB_HOST_SUBBATCHES = p > 0 cuts p equal parts; by default
+    // the sizes ramp up and down (1, 3, 4, 4, 3, 1 sixteenths of the input),
+    // so that the kernels start after a short first copy and the last copy
+    // out is short (the pipeline's fill and drain); each part >= 256 MB.
+    const int parts = env_int("MGB_HOST_SUBBATCHES", 0);
+    std::vector<double> weights;
+    if (parts > 0) weights.assign((size_t)parts, 1.0);
+    else weights = {1, 3, 4, 4, 3, 1};
+    double wsum = 0.0;
+    for (double w : weights) wsum += w;
     std::vector<size_t> cut{0};
-    for (size_t i = 0, acc = 0; i < count; ++i) {
-        if (acc > 0 && acc + bin[i] > target) {
-            cut.push_back(i);
-            acc = 0;
+    {
+        const size_t minb = (size_t)256 << 20;
+        double bound = 0.0;
+        size_t k = 0, acc = 0, in_part = 0;
+        bound = (double)total * weights[0] / wsum;
+        for (size_t i = 0; i < count; ++i) {
+            acc += bin[i];
+            in_part += bin[i];
+            if (i + 1 < count && k + 1 < weights.size() && (double)acc >= bound && in_part >= minb) {
+                cut.push_back(i + 1);
+                in_part = 0;
+                ++k;
+                bound += (double)total * weights[k] / wsum;
+            }
         }
-        acc += bin[i];
     }
     cut.push_back(count);
     const size_t nb = cut.size() - 1;
@@ -1389,8 +1408,12 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
         if (st == MGB_OK) st = plan_streams(u.pc);
         if (st != MGB_OK) break;
         if (used[k]) e = cudaStreamWaitEvent(sin, ev_out[k], 0);
+        char nm_in[32], nm_comp[32], nm_out[32];
+        std::snprintf(nm_in, sizeof nm_in, "h2d.%zu", b);
+        std::snprintf(nm_comp, sizeof nm_comp, "comp.%zu", b);
+        std::snprintf(nm_out, sizeof nm_out, "d2h.%zu", b);
         if (e == cudaSuccess)
-            e = timed("h2d", sin, [&] {
+            e = timed(nm_in, sin, [&] {
                 cudaError_t r = cudaSuccess;
                 for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
                     r = stage_copy(const_cast<void*>(u.in[j]), A[i0 + j], bin[i0 + j], true, sms, sin);
@@ -1404,13 +1427,20 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
             st = cuda_fail(e);
             break;
         }
-        st = plan_forward(u.pc, scomp);
-        if (st == MGB_OK) st = plan_vjp(u.pc, scomp, false);
+        e = timed(nm_comp, scomp, [&] {
+            st = plan_forward(u.pc, scomp);
+            if (st == MGB_OK) st = plan_vjp(u.pc, scomp, false);
+            return cudaSuccess;
+        });
         if (st != MGB_OK) break;
+        if (e != cudaSuccess) {
+            st = cuda_fail(e);
+            break;
+        }
         e = cudaEventRecord(ev_comp[k], scomp);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sout, ev_comp[k], 0);
         if (e == cudaSuccess)
-            e = timed("d2h", sout, [&] {
+            e = timed(nm_out, sout, [&] {
                 cudaError_t r = cudaSuccess;
                 for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
                     r = stage_copy(out[i0 + j], u.out[j], bout[i0 + j], false, sms, sout);
@@ -1476,6 +1506,10 @@ const char* mgb_last_error(void) { return g_last_error.c_str(); }
 
 mgb_status mgb_profile_enable(int enable) {
     std::lock_guard<std::mutex> lock(g_prof_mutex);
+    if (enable && !g_prof_enabled) {
+        if (!g_prof_ref && cudaEventCreate(&g_prof_ref) != cudaSuccess) g_prof_ref = nullptr;
+        if (g_prof_ref) cudaEventRecord(g_prof_ref, nullptr);
+    }
     g_prof_enabled = enable != 0;
     return MGB_OK;
 }
@@ -1493,6 +1527,12 @@ size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset) {
             }
             it->second.launches += 1;
             it->second.ms += ms;
+            float t0 = 0.f, t1 = 0.f;
+            if (g_prof_ref && cudaEventElapsedTime(&t0, g_prof_ref, ev.start) == cudaSuccess &&
+                cudaEventElapsedTime(&t1, g_prof_ref, ev.stop) == cudaSuccess) {
+                it->second.first = std::min(it->second.first, (double)t0);
+                it->second.last = std::max(it->second.last, (double)t1);
+            }
         }
         cudaEventDestroy(ev.start);
         cudaEventDestroy(ev.stop);
@@ -1504,6 +1544,8 @@ size_t mgb_profile_read(mgb_kernel_time* out, size_t capacity, int reset) {
         std::strncpy(out[i].name, g_prof_totals[i].first.c_str(), sizeof(out[i].name) - 1);
         out[i].launches = g_prof_totals[i].second.launches;
         out[i].total_ms = g_prof_totals[i].second.ms;
+        out[i].first_start_ms = g_prof_totals[i].second.first;
+        out[i].last_end_ms = g_prof_totals[i].second.last;
     }
     if (reset) g_prof_totals.clear();
     return count;

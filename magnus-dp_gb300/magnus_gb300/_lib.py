@@ -45,7 +45,8 @@ class Problem(ctypes.Structure):
 
 
 class KernelTime(ctypes.Structure):
-    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double)]
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double),
+                ("first_start_ms", ctypes.c_double), ("last_end_ms", ctypes.c_double)]
 
 
 # name -> (restype, argtypes) for every symbol the header declares
@@ -79,11 +80,13 @@ SIGNATURES = {
 
 
 def profile_read(reset=True):
-    """{kernel name: (launches, total_ms)} recorded since the last reset."""
+    """{name: (launches, total_ms, first_start_ms, last_end_ms)} recorded
+    since the last reset (times after the moment timing was switched on)."""
     lib = load()
-    buf = (KernelTime * 64)()
-    count = lib.mgb_profile_read(buf, 64, int(reset))
-    return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].total_ms)) for i in range(min(count, 64))}
+    buf = (KernelTime * 256)()
+    count = lib.mgb_profile_read(buf, 256, int(reset))
+    return {buf[i].name.decode(): (int(buf[i].launches), float(buf[i].total_ms), float(buf[i].first_start_ms),
+                                   float(buf[i].last_end_ms)) for i in range(min(count, 256))}
 
 _lib = None
 

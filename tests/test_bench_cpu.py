@@ -35,3 +35,20 @@ def test_reference_arm_json_line():
 
 def test_reference_arm_other_ranks_are_silent():
     assert _run({"RANK": "1"}) == []
+
+
+def test_kernel_roofs_from_profile_records():
+    """The per-kernel roofline of the JSON line from the library's timing
+    records ({name: (launches, total_ms, first_start_ms, last_end_ms)}): the
+    config4 chunk kernels are rated against the tensor roof, the mixed-form
+    scans against double-FP32, and every fraction is achieved / peak."""
+    sys.path.insert(0, ROOT)
+    import bench
+    rec = {"chunk_local": (3, 420.0, 0.0, 1.0), "chunk_vjp": (3, 1170.0, 0.0, 1.0), "scan": (3, 39.7, 0.0, 1.0),
+           "rscan": (3, 39.8, 0.0, 1.0), "fin_fwd": (3, 9.6, 0.0, 1.0)}
+    roofs = bench.kernel_roofs(rec, 3, 512, 32769, 32, 5, 256)
+    vjp = roofs["chunk_vjp"]
+    assert vjp["bound"] == "tensor" and abs(vjp["launch_ms"] - 390.0) < 1e-9
+    assert abs(vjp["achieved"] - 3 * 4 * 2 * 32 ** 3 * 32769 * 512 / 0.39 / 1e12) < 1e-6
+    assert abs(vjp["frac"] - vjp["achieved"] / vjp["peak"]) < 1e-12
+    assert roofs["scan"]["bound"] == "fp32" and roofs["fin_fwd"]["bound"] == "hbm"

@@ -287,3 +287,36 @@ def test_mixed_long_four_element_problems_use_long_chunks(cuda):
     gref = O.vjp_sc(F, cot, 6, 0.0, 2.0, "many", "Simpson")
     g = core.compute_sc_vjp(6, F, cot, t0=0.0, tf=2.0, op="many", integrator="Simpson", precision="mixed")
     assert rel(g, gref) <= 1e-6, rel(g, gref)
+
+
+@pytest.mark.parametrize("integrator,S", [("Boole", 1025), ("Simpson", 1023), ("Trapezoid", 1023), ("Riemann", 1000)])
+def test_mma32_scale_jumps(integrator, S, cuda, monkeypatch):
+    """The d = 32 warp-MMA kernel predicts each operand's power-of-two scale
+    from the previous group and re-splits when the prediction misses.  Here
+    A(t) is zero on the first third of the samples, jumps to a scale 1e3
+    larger on the middle third and back down: every operand (A, the prefixes
+    P_j, the cotangents G_j) jumps by orders of magnitude between groups, in
+    both directions, at chunk boundaries and inside chunks.  Every order stays
+    within 1e-6; dA on this input is at the mixed form's own floor (about
+    2.3e-6, as the FP32 SIMT kernel measures it), so the warp-MMA variants'
+    dA is held to that kernel's error."""
+    d, n = 32, 4
+    A = smooth_samples(S, d, seed=77)
+    A[: S // 3] = 0.0
+    A[S // 3: 2 * S // 3] *= 1e3
+    A = A.astype(np.float32)
+    A64 = A.astype(np.float64)
+    ref = O.forward(A64, n, 0.0, 1.0, "many", integrator)
+    cot = np.random.default_rng(5).standard_normal((d, d)).astype(np.float32)
+    gref = O.vjp(A64, cot.astype(np.float64), n, 0.0, 1.0, "sum", integrator)
+    err = {}
+    for variant in (0, 2, 3):
+        monkeypatch.setenv("MGB_FORCE_VARIANT", str(variant))
+        out = core.compute(n, A, 0.0, 1.0, op="many", integrator=integrator, precision="mixed", checkpoint_K=64)
+        for k in range(n):
+            assert rel(out[k], ref[k]) <= 1e-6, (variant, k, rel(out[k], ref[k]))
+        g = core.compute_vjp(n, A, cot, t0=0.0, tf=1.0, op="sum", integrator=integrator, precision="mixed",
+                             checkpoint_K=64)
+        err[variant] = rel(g, gref)
+    assert err[0] <= 5e-6, err
+    assert err[2] <= 1.25 * err[0] + 1e-7 and err[3] <= 1.25 * err[0] + 1e-7, err
