@@ -669,18 +669,25 @@ __global__ void __launch_bounds__(NT, 2)
                             if (so <= gg) {
                                 const int k = mx_get(so);
                                 const float sc = pow2f(k);
-                                if (nxt && so < gg && !(noa && so == 0)) {
+                                const bool tox = nxt && so < gg && !(noa && so == 0), tot = so >= 1;
+                                // one split, stored to both destinations
 #pragma unroll
-                                    for (int q = 0; q < NP; ++q)
-                                        put_pair(xb + so * SET, prow(q), pcol(q), Pk[q][0][so], Pk[q][1][so], sc);
-                                    if (tid == 0) sk[SK_B + so] = k;
+                                for (int q = 0; q < NP; ++q) {
+                                    if (!tox && !tot) break;
+                                    uint32_t p0, p1;
+                                    split2(Pk[q][0][so], Pk[q][1][so], sc, p0, p1);
+                                    const uint32_t o = toff(prow(q), pcol(q));
+                                    if (tox) {
+                                        *reinterpret_cast<uint32_t*>(xb + so * SET + o) = p0;
+                                        *reinterpret_cast<uint32_t*>(xb + so * SET + PT + o) = p1;
+                                    }
+                                    if (tot) {
+                                        *reinterpret_cast<uint32_t*>(gj + (so - 1) * SET + o) = p0;
+                                        *reinterpret_cast<uint32_t*>(gj + (so - 1) * SET + PT + o) = p1;
+                                    }
                                 }
-                                if (so >= 1) {
-#pragma unroll
-                                    for (int q = 0; q < NP; ++q)
-                                        put_pair(gj + (so - 1) * SET, prow(q), pcol(q), Pk[q][0][so], Pk[q][1][so], sc);
-                                    if (tid == 0) gtk[(j - 1) * G + so - 1] = k;
-                                }
+                                if (tid == 0 && tox) sk[SK_B + so] = k;
+                                if (tid == 0 && tot) gtk[(j - 1) * G + so - 1] = k;
                             }
                         }
                         mx_done();

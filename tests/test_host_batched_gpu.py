@@ -83,3 +83,37 @@ def test_rejects_null_buffers(cuda):
     probs = _probs([(2, 129, 3)], _lib.PRECISION_PLAIN, _lib.DTYPE_F64)
     st = lib.mgb_fwd_vjp_host_batched(probs, 1, _arr([None]), _arr([None]), _arr([None]), _arr([None]))
     assert st == 1 and b"must not be null" in lib.mgb_last_error()
+
+
+def test_profile_timeline_of_the_pipeline(cuda):
+    """With timing on, each sub-batch's stages are recorded as h2d.<b>,
+    comp.<b>, d2h.<b> with start and end times: every stage starts after the
+    one it depends on has ended (copy in -> kernels -> copy out)."""
+    import torch
+    lib = _lib.load()
+    specs = [(32, 4097, 4)] * 36  # ~0.6 GB of input: more than one sub-batch
+    A_h = [torch.tensor(workloads.config0_samples(seed=k, d=d, samples=S).astype(np.float32)).pin_memory()
+           for k, (d, S, n) in enumerate(specs)]
+    cot_h = [torch.ones((d, d), dtype=torch.float32).pin_memory() for d, S, n in specs]
+    out_h = [torch.empty((d, d), dtype=torch.float32).pin_memory() for d, S, n in specs]
+    dA_h = [torch.empty_like(a).pin_memory() for a in A_h]
+    probs = _probs(specs, _lib.PRECISION_MIXED, _lib.DTYPE_F32)
+    args = (probs, len(specs), _arr([t.data_ptr() for t in A_h]), _arr([t.data_ptr() for t in cot_h]),
+            _arr([t.data_ptr() for t in out_h]), _arr([t.data_ptr() for t in dA_h]))
+    _lib.check(lib.mgb_fwd_vjp_host_batched(*args))
+    lib.mgb_profile_enable(1)
+    _lib.profile_read(reset=True)
+    try:
+        _lib.check(lib.mgb_fwd_vjp_host_batched(*args))
+    finally:
+        lib.mgb_profile_enable(0)
+    rec = _lib.profile_read(reset=True)
+    subs = sorted(int(k.split(".")[1]) for k in rec if k.startswith("comp."))
+    assert len(subs) >= 2, sorted(rec)
+    eps = 1e-3  # ms
+    for b in subs:
+        h, c, o = rec[f"h2d.{b}"], rec[f"comp.{b}"], rec[f"d2h.{b}"]
+        for launches, total, start, end in (h, c, o):
+            assert launches == 1 and end >= start and abs((end - start) - total) <= 1e-2 * max(total, 1.0)
+        assert c[2] >= h[3] - eps and o[2] >= c[3] - eps, (b, h, c, o)
+    assert any(k.startswith("chunk") for k in rec), sorted(rec)
