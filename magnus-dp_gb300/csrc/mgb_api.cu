@@ -530,6 +530,8 @@ void plan_fill(const Call& call, PlanCore& pc, const std::vector<Derived>& dv) {
         for (int c = 0; c < v.C; ++c) pc.work.push_back(ChunkRef{(int32_t)k, c});
     }
     for (Segment& sg : pc.segs) {
+        // double-FP32 scans read the chunk kernels' transfer pairs directly
+        for (int32_t k = sg.first; k < sg.first + sg.count; ++k) pc.hi[k].lam_pair = sg.df_scan ? 1 : 0;
         sg.hi.assign(pc.hi.begin() + sg.first, pc.hi.begin() + sg.first + sg.count);
         sg.tc = TunedChoice{};
     }

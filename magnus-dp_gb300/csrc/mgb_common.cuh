@@ -74,7 +74,10 @@ struct InstDev {
     double sig;
     int64_t S;
     int32_t d, m, n, C, Q, K, op;
-    int32_t pad_;
+    // 1: lam holds each transfer element as the chunk kernel's unevaluated
+    // FP32 pair (hi, lo) in its 8 bytes (segments whose scans run in
+    // double-FP32 read the pair as it is, with no FP64 conversions); 0: FP64
+    int32_t lam_pair;
     // The rule coefficients of dt_k (RuleCoef's order), computed once on the
     // host by rule_coefs(): FP64 divisions in every thread of every chunk
     // took a large share of the 1/64-rate FP64 pipe.
@@ -82,6 +85,12 @@ struct InstDev {
     float rcf[9];
     int32_t pad2_;
 };
+
+// Store element idx of the chunk transfers (a local prefix total hi + lo).
+__device__ __forceinline__ void store_lam(const InstDev& I, int64_t idx, float hi, float lo) {
+    if (I.lam_pair) reinterpret_cast<float2*>(I.lam)[idx] = make_float2(hi, lo);
+    else I.lam[idx] = (double)hi + (double)lo;
+}
 
 // h, t3, c38, c98, c4_3, b14, b64, b24, dt of a step (host and device).
 __host__ __device__ inline void rule_coefs(double dtd, double* c) {

@@ -426,8 +426,8 @@ __global__ void __launch_bounds__(NT, 2)
         if (alive) {
             for (int j = 1; j <= n; ++j)
                 for (int el = tid; el < m; el += NT)
-                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] =
-                        (double)st[(j - 1) * 3 * m + el] + (double)st[(j - 1) * 3 * m + m + el];
+                    store_lam(I, (int64_t)c * nm + (int64_t)(j - 1) * m + el, st[(j - 1) * 3 * m + el],
+                              st[(j - 1) * 3 * m + m + el]);
         }
         }  // MODE_LOCAL
 

@@ -109,8 +109,18 @@ __global__ void __launch_bounds__(SNTD) k_scan_df(const InstDev* __restrict__ in
 
     for (int step = 0; step < (REV ? C - 1 : C); ++step) {
         const int c = REV ? C - 1 - step : step;  // transfer Lambda^c
-        const double* lc = I.lam + (int64_t)c * nm;
-        for (int i = tid; i < nm; i += SNTD) df_split(lc[i], lh[i], ll[i]);
+        if (I.lam_pair) {
+            // the chunk kernel's FP32 pairs as they are (no FP64 work)
+            const float2* lc = reinterpret_cast<const float2*>(I.lam) + (int64_t)c * nm;
+            for (int i = tid; i < nm; i += SNTD) {
+                const float2 v = lc[i];
+                lh[i] = v.x;
+                ll[i] = v.y;
+            }
+        } else {
+            const double* lc = I.lam + (int64_t)c * nm;
+            for (int i = tid; i < nm; i += SNTD) df_split(lc[i], lh[i], ll[i]);
+        }
         __syncthreads();
         for (int it = 0; it < n; ++it) {
             const int j = REV ? 1 + it : n - it;  // level updated in place

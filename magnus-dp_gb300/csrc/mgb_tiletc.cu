@@ -258,8 +258,8 @@ __global__ void __launch_bounds__(TT, 2)
             for (int j = 1; j <= n; ++j)
                 for (int q = 0; q < m / TT; ++q) {
                     const int el = tid + q * TT;
-                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] =
-                        (double)st[(j - 1) * 3 * m + el] + (double)st[(j - 1) * 3 * m + m + el];
+                    store_lam(I, (int64_t)c * nm + (int64_t)(j - 1) * m + el, st[(j - 1) * 3 * m + el],
+                              st[(j - 1) * 3 * m + m + el]);
                 }
         }
         __syncthreads();

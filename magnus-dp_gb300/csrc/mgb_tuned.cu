@@ -282,8 +282,8 @@ __global__ void __launch_bounds__(TNT, MINB) k_tile(const InstDev* __restrict__ 
             for (int j = 1; j <= n; ++j)
                 for (int q = 0; q < EPT; ++q) {
                     const int el = tid + q * TNT;
-                    I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] =
-                        (double)st[(j - 1) * 3 * m + el] + (double)st[(j - 1) * 3 * m + m + el];
+                    store_lam(I, (int64_t)c * nm + (int64_t)(j - 1) * m + el, st[(j - 1) * 3 * m + el],
+                              st[(j - 1) * 3 * m + m + el]);
                 }
         }
 
