@@ -82,7 +82,7 @@ static_assert(NP * 2 * NT == m, "pair mapping");
 static_assert(m / 4 == NT, "one quad of every sample per thread");
 static_assert(SMEM + 1024 <= 114 * 1024, "two CTAs per SM");
 
-// One warp: acc (main, small) [mt][nt] += (X Y)[:, 16 nh .. 16 nh + 15] for
+// One warp: acc (main, small) [mt][nt] = (X Y)[:, 16 nh .. 16 nh + 15] for
 // one sample (scaled), X and Y 32 x 32 given as FP16 piece tiles (NPC tiles,
 // PT bytes apart) in row-major storage S:
 //   XT = false: X = S_x (rows m, cols k);  XT = true: X = S_x^T
@@ -131,13 +131,21 @@ __device__ __forceinline__ void warp_product(uint32_t xs, uint32_t ys, float (&a
 #pragma unroll
             for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                for (int nt = 0; nt < 2; ++nt)
-                    mma16816(q == 2 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0], bf[PJ[q]][nt][1]);
+                for (int nt = 0; nt < 2; ++nt) {
+                    // each accumulator's first MMA (k-step 0: the first small
+                    // term, the main term) starts from zero
+                    if (ks == 0 && q != 1)
+                        mma16816_first(q == 2 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0],
+                                       bf[PJ[q]][nt][1]);
+                    else
+                        mma16816(q == 2 ? am[mt][nt] : as[mt][nt], af[PI[q]][mt], bf[PJ[q]][nt][0], bf[PJ[q]][nt][1]);
+                }
     }
 }
 
-// Factors undoing the operand scales 2^kx, 2^ky: v * u.a * u.b (two factors
-// keep each one a normal float)
+// Factors undoing the operand scales 2^kx, 2^ky: v * u.a, then * u.b when
+// kx + ky is outside the normal exponent range (u.b != 1; two factors keep
+// each one a normal float).  u.b is the same for a whole warp.
 struct Unscale {
     float a, b;
 };
@@ -145,6 +153,7 @@ __device__ __forceinline__ Unscale unscale(int kx, int ky) {
     const int k = kx + ky, k1 = min(126, max(-126, k));
     return Unscale{pow2f(-k1), pow2f(k1 - k)};
 }
+__device__ __forceinline__ float apply(float v, const Unscale& u, bool two) { return two ? v * u.a * u.b : v * u.a; }
 
 __device__ __forceinline__ void zero_acc(float (&a)[2][2][4]) {
 #pragma unroll
@@ -159,15 +168,16 @@ __device__ __forceinline__ void zero_acc(float (&a)[2][2][4]) {
 // sw (pitch WP)
 __device__ __forceinline__ void store_acc(float* o, const float (&am)[2][2][4], const float (&as)[2][2][4], int g8,
                                           int t4, int nh, Unscale u) {
+    const bool two = u.b != 1.f;
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
         for (int nt = 0; nt < 2; ++nt) {
             const int r = mt * 16 + g8, cc = (2 * nh + nt) * 8 + 2 * t4;
             *reinterpret_cast<float2*>(o + r * WP + cc) =
-                make_float2((am[mt][nt][0] + as[mt][nt][0]) * u.a * u.b, (am[mt][nt][1] + as[mt][nt][1]) * u.a * u.b);
+                make_float2(apply(am[mt][nt][0] + as[mt][nt][0], u, two), apply(am[mt][nt][1] + as[mt][nt][1], u, two));
             *reinterpret_cast<float2*>(o + (r + 8) * WP + cc) =
-                make_float2((am[mt][nt][2] + as[mt][nt][2]) * u.a * u.b, (am[mt][nt][3] + as[mt][nt][3]) * u.a * u.b);
+                make_float2(apply(am[mt][nt][2] + as[mt][nt][2], u, two), apply(am[mt][nt][3] + as[mt][nt][3], u, two));
         }
 }
 
@@ -413,8 +423,6 @@ __global__ void __launch_bounds__(NT, 2)
                     load_fstate(j + 1);
                     if (ws < ge) {
                         float am[2][2][4], as[2][2][4];
-                        zero_acc(am);
-                        zero_acc(as);
                         warp_product<false, false>(sxa + ws * SET, sxb + ws * SET, am, as, lane, nh);
                         store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh, unscale(sk[ws], sk[SK_B + ws]));
                     }
@@ -560,8 +568,6 @@ __global__ void __launch_bounds__(NT, 2)
                         // W_j = A P_{j-1} at offsets 0..ge-1 (samples a .. a + ge - 1)
                         if (ws < ge && !(noa && ws == 0)) {
                             float am[2][2][4], as[2][2][4];
-                            zero_acc(am);
-                            zero_acc(as);
                             warp_product<false, false>(sxa + ring(a + ws) * SET, sxb + ws * SET, am, as, lane, nh);
                             store_acc(sw + ws * 32 * WP, am, as, g8, t4, nh, unscale(sk[ring(a + ws)], sk[SK_B + ws]));
                         }
@@ -712,21 +718,28 @@ __global__ void __launch_bounds__(NT, 2)
                             // H_j = A^T G_{j+1} -> sw;  dA += G_{j+1} P_j^T
                             const int kp = gtk[(j - 1) * G + ws];
                             float hm[2][2][4], hs[2][2][4];
-                            zero_acc(hm);
-                            zero_acc(hs);
                             warp_product<true, false>(xas, sxb + ws * SET, hm, hs, lane, nh);
                             store_acc(sw + ws * 32 * WP, hm, hs, g8, t4, nh, unscale(sk[ring(li0 + ws)], sk[SK_B + ws]));
                             float tm[2][2][4], ts[2][2][4];
-                            zero_acc(tm);
-                            zero_acc(ts);
                             warp_product<false, true>(sxb + ws * SET, sxc + ws * SET, tm, ts, lane, nh);
                             const Unscale u = unscale(sk[SK_B + ws], kp);
+                            if (u.b == 1.f) {
 #pragma unroll
-                            for (int mt = 0; mt < 2; ++mt)
+                                for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-                                for (int nt = 0; nt < 2; ++nt)
+                                    for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
-                                    for (int k = 0; k < 4; ++k) da[mt][nt][k] += (tm[mt][nt][k] + ts[mt][nt][k]) * u.a * u.b;
+                                        for (int k = 0; k < 4; ++k)
+                                            da[mt][nt][k] = fmaf(tm[mt][nt][k] + ts[mt][nt][k], u.a, da[mt][nt][k]);
+                            } else {
+#pragma unroll
+                                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                                    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                                        for (int k = 0; k < 4; ++k)
+                                            da[mt][nt][k] += (tm[mt][nt][k] + ts[mt][nt][k]) * u.a * u.b;
+                            }
                         }
                     }
                     __syncthreads();
