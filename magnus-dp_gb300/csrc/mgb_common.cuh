@@ -87,9 +87,15 @@ struct InstDev {
 };
 
 // Store element idx of the chunk transfers (a local prefix total hi + lo).
+// Every chunk kernel of a segment goes through this (the scans of a
+// double-FP32 segment read pairs whichever kernel ran); FP64 totals (the
+// plain form, whose scans are FP64) are stored as they are.
 __device__ __forceinline__ void store_lam(const InstDev& I, int64_t idx, float hi, float lo) {
     if (I.lam_pair) reinterpret_cast<float2*>(I.lam)[idx] = make_float2(hi, lo);
     else I.lam[idx] = (double)hi + (double)lo;
+}
+__device__ __forceinline__ void store_lam(const InstDev& I, int64_t idx, double hi, double lo) {
+    I.lam[idx] = hi + lo;
 }
 
 // h, t3, c38, c98, c4_3, b14, b64, b24, dt of a step (host and device).

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(NT) k_chunk(const InstDev* __restrict__ insts,
                     const T P = fwd_step<T, RULE>(s, F[(int64_t)li * m + el], li, kc, cy);
                     if (keep) Pj[(int64_t)li * m + el] = P;
                 }
-                if (MODE == MODE_LOCAL) I.lam[(int64_t)c * nm + (int64_t)(j - 1) * m + el] = (double)s.base + (double)s.blo;
+                if (MODE == MODE_LOCAL) store_lam(I, (int64_t)c * nm + (int64_t)(j - 1) * m + el, s.base, s.blo);
             }
             __syncthreads();
             if (j < n) {
