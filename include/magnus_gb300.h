@@ -149,7 +149,11 @@ mgb_status mgb_vjp_host(const mgb_problem* p, const void* A, const void* cot, vo
  * previous one and the device-to-host copy of the one before overlap.  Host
  * buffers should be page-locked (cudaHostAlloc / cudaMallocHost / torch
  * pin_memory) for the copies to overlap; pageable ones are correct but
- * staged by the driver.  The slots stay allocated on
+ * staged by the driver.  With page-locked buffers the inputs of the first
+ * two sub-batches and the dA of the last two are moved by a copy kernel
+ * through the host mapping (the pipeline's fill and drain, when the copy
+ * engines alone were slow on the GB300's host link), the rest by the copy
+ * engines.  The slots stay allocated on
  * the device for later calls (calls are serialized inside the library). */
 mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, const void* const* A,
                                     const void* const* cot, void* const* out, void* const* dA);

@@ -944,13 +944,42 @@ struct mgb_plan {
 // ---------------------------------------------------------------- host staging
 namespace {
 
-// Host <-> device copy on stream s through the copy engines: asynchronous for
-// page-locked host buffers, staged by the driver for pageable ones.  (A copy
-// kernel reading mapped host memory measured the same link bandwidth on the
-// GB300 — 211 GB/s in, 194 GB/s out — but took SM slots from the chunk
-// kernels running beside it.)
-cudaError_t stage_copy(void* dst, const void* src, size_t bytes, bool to_device, int, cudaStream_t s) {
+// SM-driven copy of n4 16-byte words (host side through its device mapping).
+__global__ void k_stage_copy(const float4* __restrict__ src, float4* __restrict__ dst, size_t n4) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// Device address of a page-locked host buffer (nullptr for pageable memory).
+const void* mapped_host(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Host <-> device copy on stream s: through the copy engines (asynchronous
+// for page-locked host buffers, staged by the driver for pageable ones), or,
+// with sm and a page-locked, 16-byte aligned host buffer, by a copy kernel
+// reading or writing the host memory through its mapping.  On the GB300 host
+// link the copy engines moved 14-65 GB/s while no kernel was running (the
+// pipeline's fill and drain) against about 210 GB/s beside the kernels; the
+// copy kernel keeps about 120-210 GB/s there, at the cost of SM slots, so the
+// pipeline uses it only at its two ends.
+cudaError_t stage_copy(void* dst, const void* src, size_t bytes, bool to_device, int sms, cudaStream_t s,
+                       bool sm = false) {
     if (bytes == 0) return cudaSuccess;
+    if (sm && bytes % 16 == 0 && (uintptr_t)src % 16 == 0 && (uintptr_t)dst % 16 == 0) {
+        const void* hp = mapped_host(to_device ? src : dst);
+        if (hp) {
+            const float4* from = static_cast<const float4*>(to_device ? hp : src);
+            float4* to = static_cast<float4*>(to_device ? dst : const_cast<void*>(hp));
+            k_stage_copy<<<(unsigned)std::max(sms, 1), 512, 0, s>>>(from, to, bytes / 16);
+            return cudaGetLastError();
+        }
+    }
     return cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, s);
 }
 
@@ -1418,7 +1447,7 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
             e = timed(nm_in, sin, [&] {
                 cudaError_t r = cudaSuccess;
                 for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
-                    r = stage_copy(const_cast<void*>(u.in[j]), A[i0 + j], bin[i0 + j], true, sms, sin);
+                    r = stage_copy(const_cast<void*>(u.in[j]), A[i0 + j], bin[i0 + j], true, sms, sin, b < 2);
                     if (r == cudaSuccess) r = stage_copy(const_cast<void*>(u.cot[j]), cot[i0 + j], bout[i0 + j], true, sms, sin);
                 }
                 return r;
@@ -1446,7 +1475,7 @@ mgb_status mgb_fwd_vjp_host_batched(const mgb_problem* probs, size_t count, cons
                 cudaError_t r = cudaSuccess;
                 for (size_t j = 0; j < cnt && r == cudaSuccess; ++j) {
                     r = stage_copy(out[i0 + j], u.out[j], bout[i0 + j], false, sms, sout);
-                    if (r == cudaSuccess) r = stage_copy(dA[i0 + j], u.dA[j], bin[i0 + j], false, sms, sout);
+                    if (r == cudaSuccess) r = stage_copy(dA[i0 + j], u.dA[j], bin[i0 + j], false, sms, sout, b + 2 >= nb);
                 }
                 return r;
             });
