@@ -119,6 +119,18 @@ def config4_samples_torch(Ck, samples=32769, t0=0.0, tf=1.0, dtype=None, device=
     return out
 
 
+def config4_poly_samples(seed=44, samples=32769, d=32, t0=0.0, tf=1.0):
+    """One trajectory of config4's shape with A(t) = C0 + t (C1 + t (C2 + t
+    C3)), C_k ~ N(0, 1/d) seeded: evaluated with elementwise float64 + and *
+    only, so bit-identical on every platform, then rounded to float32 and
+    returned as float64 (the exact float32 values)."""
+    rng = np.random.default_rng(seed)
+    C = rng.standard_normal((4, d, d)) * np.sqrt(1.0 / d)
+    t = np.linspace(t0, tf, samples)[:, None, None]
+    A = C[0] + t * (C[1] + t * (C[2] + t * C[3]))
+    return A.astype(np.float32).astype(np.float64)
+
+
 def config4_cotangent(seed=40, batch=512, d=32, dtype=np.float32):
     rng = np.random.default_rng(seed)
     return rng.standard_normal((batch, d, d)).astype(dtype)

@@ -171,6 +171,27 @@ def complex_cases():
     return cases
 
 
+def config4_full_cases():
+    """One full trajectory of config4's shape (d = 32, S = 32769, n = 5,
+    Boole) run by the reference in FP64: every order (op many) and dA of op
+    sum at 39 sample indices (the ends, chunk boundaries of the engine's
+    256-sample checkpoints, and evenly spaced ones).  The samples are a cubic
+    polynomial in t with seeded coefficients, rounded to float32, so that the
+    tests regenerate them bit for bit on any machine (only +, *, and the
+    float32 cast; the benchmark's cos term would depend on the platform's
+    libm); the 268 MB of samples are not stored."""
+    d, S, n = 32, 32769, 5
+    A64 = workloads.config4_poly_samples(seed=44, samples=S, d=d)
+    out = core.compute(n, A64, 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole", gl_backend="serial")
+    cot = workloads.config4_cotangent(batch=1, d=d)[0].astype(np.float64)
+    dA = core.compute_vjp(n, A64, cot, t0=0.0, tf=1.0, op="sum", matrix_backend="Manual", integrator="Boole")
+    idx = sorted(set([0, 1, 2, 3, 4, 255, 256, 257, 258, 511, 512, 513, 16384, 16385, S - 2, S - 1]
+                     + [int(v) for v in np.linspace(0, S - 1, 25)]))
+    return {"c4full": dict(kind="matrix", integrator="Boole", op="many", n=n, t0=0.0, tf=1.0, seed=44, samples=S,
+                           dim=d, out=out, cot=cot, idx=np.array(idx), dA_rows=dA[idx],
+                           dA_norm=np.linalg.norm(dA))}
+
+
 def save(name, cases):
     flat = {}
     for key, c in cases.items():
@@ -181,7 +202,7 @@ def save(name, cases):
 
 def main():
     makers = {"small.npz": small_cases, "medium.npz": medium_cases, "config0.npz": config0_cases,
-              "float32.npz": float32_cases, "complex.npz": complex_cases}
+              "float32.npz": float32_cases, "complex.npz": complex_cases, "config4_full.npz": config4_full_cases}
     for name in (sys.argv[1:] or makers):  # e.g. `make_golden.py complex.npz` regenerates one file
         save(name, makers[name]())
     for f in sorted(os.listdir(HERE)):

@@ -1,13 +1,15 @@
 """Pins the collapsed FP64 checker (oracle/collapsed.py) against the C oracle
-(the reference's per-node recursion restated) on every rule and op, so that
-the full-size GPU parity tests can use it where the C oracle would take
-minutes per instance."""
+(the reference's per-node recursion restated) on every rule and op, and
+against the reference's own outputs at config4's size, so that the
+full-size GPU parity tests can use it where the C oracle would take minutes
+per instance."""
 import numpy as np
 import pytest
 
 import collapsed as Cl
 import oracle as O
-from conftest import rel
+from conftest import load_cases, rel
+from magnus_gb300 import workloads
 
 RULES = [("Boole", 129), ("Simpson", 131), ("Trapezoid", 97), ("Riemann", 90)]
 
@@ -46,3 +48,20 @@ def test_prefix_transpose_is_the_adjoint(rule, S):
     lhs = np.sum(Cl.prefix(f, 0.01, rule) * h)
     rhs = np.sum(f * Cl.prefix_t(h, 0.01, rule))
     assert abs(lhs - rhs) <= 1e-13 * max(1.0, abs(lhs))
+
+
+def test_collapsed_checker_matches_reference_at_config4_size():
+    """The FP64 checker the full-size GPU parity tests use, against the
+    reference itself at config4's size (tests/golden/config4_full.npz: the
+    reference's every order and its dA at 39 sample indices for one d = 32,
+    S = 32769, n = 5 Boole trajectory with platform-independent samples)."""
+    g = load_cases("config4_full.npz")["c4full"]
+    n, S, d = int(g["n"]), int(g["samples"]), int(g["dim"])
+    A64 = workloads.config4_poly_samples(seed=int(g["seed"]), samples=S, d=d)
+    out = Cl.forward(A64, n, 0.0, 1.0, "many", "Boole")
+    for k in range(n):
+        assert rel(out[k], g["out"][k]) <= 1e-12, (k, rel(out[k], g["out"][k]))
+    dA = Cl.vjp(A64, g["cot"], n, 0.0, 1.0, "sum", "Boole")
+    idx = g["idx"]
+    assert rel(dA[idx], g["dA_rows"]) <= 1e-12, rel(dA[idx], g["dA_rows"])
+    assert abs(np.linalg.norm(dA) / g["dA_norm"] - 1.0) <= 1e-12
