@@ -90,6 +90,17 @@ def config2_samples_torch(Sk, samples=16385, t0=0.0, tf=1.0, dtype=None, device=
     return out
 
 
+def config2_poly_samples(seed=22, samples=16385, d=64, t0=0.0, tf=1.0):
+    """One trajectory of config2's shape with the skew-symmetric A(t) = S0 +
+    t (S1 + t S2) (config2's seeded skew coefficients): elementwise float64
+    + and * only, so bit-identical on every platform (and exactly skew),
+    rounded to float32 and returned as float64."""
+    Sk = config2_coeffs(seed=seed, batch=1, d=d)[0]
+    t = np.linspace(t0, tf, samples)[:, None, None]
+    A = Sk[0] + t * (Sk[1] + t * Sk[2])
+    return A.astype(np.float32).astype(np.float64)
+
+
 # ---------------------------------------------------------------- config4
 def config4_coeffs(seed=4, batch=512, d=32):
     rng = np.random.default_rng(seed)

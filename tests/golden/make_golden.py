@@ -192,6 +192,23 @@ def config4_full_cases():
                            dA_norm=np.linalg.norm(dA))}
 
 
+def config2_full_cases():
+    """One full trajectory of config2's shape (skew-symmetric d = 64, S =
+    16385, n = 4, Boole) run by the reference in FP64, stored like
+    config4_full_cases (every order, dA at sample indices; samples a seeded
+    skew quadratic in t, regenerated bit for bit by the tests)."""
+    d, S, n = 64, 16385, 4
+    A64 = workloads.config2_poly_samples(seed=22, samples=S, d=d)
+    out = core.compute(n, A64, 0.0, 1.0, op="many", matrix_backend="Manual", integrator="Boole", gl_backend="serial")
+    cot = np.random.default_rng(23).standard_normal((d, d))
+    dA = core.compute_vjp(n, A64, cot, t0=0.0, tf=1.0, op="sum", matrix_backend="Manual", integrator="Boole")
+    idx = sorted(set([0, 1, 2, 3, 4, 255, 256, 257, 258, 8192, 8193, S - 2, S - 1]
+                     + [int(v) for v in np.linspace(0, S - 1, 17)]))
+    return {"c2full": dict(kind="matrix", integrator="Boole", op="many", n=n, t0=0.0, tf=1.0, seed=22, samples=S,
+                           dim=d, out=out, cot=cot, idx=np.array(idx), dA_rows=dA[idx],
+                           dA_norm=np.linalg.norm(dA))}
+
+
 def save(name, cases):
     flat = {}
     for key, c in cases.items():
@@ -202,7 +219,8 @@ def save(name, cases):
 
 def main():
     makers = {"small.npz": small_cases, "medium.npz": medium_cases, "config0.npz": config0_cases,
-              "float32.npz": float32_cases, "complex.npz": complex_cases, "config4_full.npz": config4_full_cases}
+              "float32.npz": float32_cases, "complex.npz": complex_cases, "config4_full.npz": config4_full_cases,
+              "config2_full.npz": config2_full_cases}
     for name in (sys.argv[1:] or makers):  # e.g. `make_golden.py complex.npz` regenerates one file
         save(name, makers[name]())
     for f in sorted(os.listdir(HERE)):

@@ -65,3 +65,16 @@ def test_collapsed_checker_matches_reference_at_config4_size():
     idx = g["idx"]
     assert rel(dA[idx], g["dA_rows"]) <= 1e-12, rel(dA[idx], g["dA_rows"])
     assert abs(np.linalg.norm(dA) / g["dA_norm"] - 1.0) <= 1e-12
+
+
+def test_collapsed_checker_matches_reference_at_config2_size():
+    """As above at config2's size (tests/golden/config2_full.npz: one
+    skew-symmetric d = 64, S = 16385, n = 4 Boole trajectory)."""
+    g = load_cases("config2_full.npz")["c2full"]
+    n, S, d = int(g["n"]), int(g["samples"]), int(g["dim"])
+    A64 = workloads.config2_poly_samples(seed=int(g["seed"]), samples=S, d=d)
+    out = Cl.forward(A64, n, 0.0, 1.0, "many", "Boole")
+    for k in range(n):
+        assert rel(out[k], g["out"][k]) <= 1e-12, (k, rel(out[k], g["out"][k]))
+    dA = Cl.vjp(A64, g["cot"], n, 0.0, 1.0, "sum", "Boole")
+    assert rel(dA[g["idx"]], g["dA_rows"]) <= 1e-12, rel(dA[g["idx"]], g["dA_rows"])

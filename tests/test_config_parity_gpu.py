@@ -159,3 +159,25 @@ def test_config4_size_against_reference_outputs(cuda):
     print(f"vs reference: plain per order {ep} dA {gp:.2e}; mixed per order {em} dA {gm:.2e}")
     assert max(ep) <= PLAIN_TOL and gp <= PLAIN_TOL, (ep, gp)
     assert max(em) <= MIXED_TOL and gm <= MIXED_TOL, (em, gm)
+
+
+def test_config2_size_against_reference_outputs(cuda):
+    """The engine against the reference's own outputs at config2's size
+    (tests/golden/config2_full.npz: one skew-symmetric d = 64, S = 16385,
+    n = 4 Boole trajectory, samples regenerated bit for bit here)."""
+    from conftest import load_cases
+    g = load_cases("config2_full.npz")["c2full"]
+    n, S, d = int(g["n"]), int(g["samples"]), int(g["dim"])
+    A64 = workloads.config2_poly_samples(seed=int(g["seed"]), samples=S, d=d)
+    A32 = A64.astype(np.float32)
+    idx = g["idx"]
+    out_p = core.compute(n, A64, 0.0, 1.0, op="many", integrator="Boole", precision="plain")
+    g_p = core.compute_vjp(n, A64, g["cot"], t0=0.0, tf=1.0, op="sum", integrator="Boole", precision="plain")
+    out_m = core.compute(n, A32, 0.0, 1.0, op="many", integrator="Boole", precision="mixed")
+    g_m = core.compute_vjp(n, A32, g["cot"].astype(np.float32), t0=0.0, tf=1.0, op="sum", integrator="Boole",
+                           precision="mixed")
+    ep, em = order_errors(out_p, g["out"]), order_errors(out_m, g["out"])
+    gp, gm = rel(g_p[idx], g["dA_rows"]), rel(g_m[idx], g["dA_rows"])
+    print(f"vs reference: plain per order {ep} dA {gp:.2e}; mixed per order {em} dA {gm:.2e}")
+    assert max(ep) <= PLAIN_TOL and gp <= PLAIN_TOL, (ep, gp)
+    assert max(em) <= MIXED_TOL and gm <= MIXED_TOL, (em, gm)
